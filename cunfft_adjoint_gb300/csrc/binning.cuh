@@ -1,0 +1,142 @@
+// binning.cuh -- counting sort of samples into grid tiles (the bucket sort in
+// front of the tiled gridding).
+//
+// A tile is a run of TL consecutive grid cells that one gridding CTA owns.
+// Each sample is binned into every tile its filter taps touch (one, or two
+// near a tile edge, because the tap span 2m is shorter than a tile), so the
+// gridding CTA of a tile finds all its contributions in one contiguous range
+// of the sorted record array and owns its cells outright: no global atomics,
+// a fixed-order flush.
+//
+//   k_bin_count   per-CTA shared histogram of tile indices -> counts[tile]
+//   k_scan_tiles  exclusive scan counts -> offsets[0..ntiles], cursor = 0
+//   k_bin_scatter per-CTA shared ranks + one global reservation per
+//                 (CTA, tile) -> records in tile order
+//
+// The tile index of a sample is an exact integer function of its input (the
+// bucket indices are bit-exact); only the order of records inside a tile
+// depends on scheduling.
+//
+// A Sampler provides `int64_t n` and
+//   __device__ void prep(int64_t i, Prep<Rec>& p)
+// filling p.nt (0..2), p.t[0..nt) and p.rec.
+#pragma once
+#include "common.cuh"
+
+namespace cuna {
+namespace {
+
+constexpr int kBinSmemTiles = 6144;  // shared histogram limit (scatter: 2 x 24 KB)
+constexpr int kScatterItems = 4;     // samples per thread in k_bin_scatter
+
+template <typename Rec> struct Prep {
+  int nt;
+  int t[2];
+  Rec rec;
+};
+
+template <class S>
+__global__ void __launch_bounds__(512) k_bin_count(S smp, int *__restrict__ counts, int ntiles) {
+  extern __shared__ int lc[];
+  const bool sm = ntiles <= kBinSmemTiles;
+  if (sm) {
+    for (int t = threadIdx.x; t < ntiles; t += blockDim.x) lc[t] = 0;
+    __syncthreads();
+  }
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < smp.n; i += stride) {
+    Prep<typename S::Rec> p;
+    smp.prep(i, p);
+    for (int q = 0; q < p.nt; ++q) {
+      if (sm) atomicAdd(&lc[p.t[q]], 1);
+      else atomicAdd(&counts[p.t[q]], 1);
+    }
+  }
+  if (sm) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < ntiles; t += blockDim.x)
+      if (lc[t]) atomicAdd(&counts[t], lc[t]);
+  }
+}
+
+// Single CTA (1024 threads): offsets[t] = sum_{u<t} counts[u], offsets[ntiles]
+// = total, cursor[t] = 0.
+__global__ void __launch_bounds__(1024) k_scan_tiles(const int *__restrict__ counts,
+                                                     int *__restrict__ offsets,
+                                                     int *__restrict__ cursor, int ntiles) {
+  __shared__ int wsum[32];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int per = (ntiles + nt - 1) / nt;
+  const int beg = min(tid * per, ntiles), end = min(beg + per, ntiles);
+  int sum = 0;
+  for (int i = beg; i < end; ++i) sum += counts[i];
+  const int lane = tid & 31, w = tid >> 5;
+  int v = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += u;
+  }
+  if (lane == 31) wsum[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    int s = lane < (nt >> 5) ? wsum[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int u = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += u;
+    }
+    wsum[lane] = s;
+  }
+  __syncthreads();
+  int run = v - sum + (w > 0 ? wsum[w - 1] : 0);
+  for (int i = beg; i < end; ++i) {
+    offsets[i] = run;
+    run += counts[i];
+    cursor[i] = 0;
+  }
+  if (tid == nt - 1) offsets[ntiles] = wsum[(nt >> 5) - 1];
+}
+
+template <class S>
+__global__ void __launch_bounds__(512) k_bin_scatter(S smp, const int *__restrict__ offsets,
+                                                     int *__restrict__ cursor,
+                                                     typename S::Rec *__restrict__ recs,
+                                                     int ntiles) {
+  typedef typename S::Rec Rec;
+  extern __shared__ int sh[];
+  int *lc = sh, *lbase = sh + ntiles;
+  const bool sm = ntiles <= kBinSmemTiles;
+  if (sm) {
+    for (int t = threadIdx.x; t < ntiles; t += blockDim.x) lc[t] = 0;
+    __syncthreads();
+  }
+  const int64_t chunk0 = (int64_t)blockIdx.x * blockDim.x * kScatterItems;
+  Prep<Rec> p[kScatterItems];
+  int rk[kScatterItems][2];
+#pragma unroll
+  for (int it = 0; it < kScatterItems; ++it) {
+    const int64_t i = chunk0 + (int64_t)it * blockDim.x + threadIdx.x;
+    p[it].nt = 0;
+    if (i < smp.n) smp.prep(i, p[it]);
+    for (int q = 0; q < p[it].nt; ++q) {
+      const int t = p[it].t[q];
+      rk[it][q] = sm ? atomicAdd(&lc[t], 1) : offsets[t] + atomicAdd(&cursor[t], 1);
+    }
+  }
+  if (sm) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < ntiles; t += blockDim.x)
+      if (lc[t]) lbase[t] = offsets[t] + atomicAdd(&cursor[t], lc[t]);
+    __syncthreads();
+  }
+#pragma unroll
+  for (int it = 0; it < kScatterItems; ++it)
+    for (int q = 0; q < p[it].nt; ++q) {
+      const int pos = sm ? lbase[p[it].t[q]] + rk[it][q] : rk[it][q];
+      recs[pos] = p[it].rec;
+    }
+}
+
+}  // namespace
+}  // namespace cuna

@@ -1,0 +1,59 @@
+// common.cuh -- complex helpers, records and small utilities shared by the
+// binning, gridding and FFT kernels of the GB300 adjoint-NFFT library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cuna {
+
+template <typename T> struct CxOf;
+template <> struct CxOf<float> { typedef float2 type; };
+template <> struct CxOf<double> { typedef double2 type; };
+
+__host__ __device__ __forceinline__ float2 cmk(float a, float b) { return make_float2(a, b); }
+__host__ __device__ __forceinline__ double2 cmk(double a, double b) { return make_double2(a, b); }
+
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { return cmk(a.x + b.x, a.y + b.y); }
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { return cmk(a.x - b.x, a.y - b.y); }
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
+  return cmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+template <typename C> __host__ __device__ __forceinline__ C cmulc(C a, C b) {
+  return cmk(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <typename C> __host__ __device__ __forceinline__ C cconj(C a) { return cmk(a.x, -a.y); }
+// i * a
+template <typename C> __host__ __device__ __forceinline__ C cmuli(C a) { return cmk(-a.y, a.x); }
+template <typename C, typename T> __host__ __device__ __forceinline__ C cscale(C a, T s) {
+  return cmk(a.x * s, a.y * s);
+}
+
+// Sorted sample record of the float path: 16 bytes, one vector load.
+//   cell : grid cell the taps are anchored on (accurate: floor(s) mod ng;
+//          compat: the reference's j)
+//   a, b : per-sample filter factors (accurate: y*E1, E2; compat: E1, E2)
+//   p    : value (compat, as float bits) or original sample index (bootstrap)
+struct __align__(16) RecF {
+  int cell;
+  float a, b;
+  int p;
+};
+// Double path: 32 bytes.
+struct __align__(16) RecD {
+  int cell;
+  int p;
+  double a, b;
+  double v;
+};
+template <typename T> struct RecOf;
+template <> struct RecOf<float> { typedef RecF type; };
+template <> struct RecOf<double> { typedef RecD type; };
+
+__host__ __device__ __forceinline__ int ilog2i(int64_t v) {
+  int r = 0;
+  while ((int64_t(1) << (r + 1)) <= v) ++r;
+  return r;
+}
+
+}  // namespace cuna

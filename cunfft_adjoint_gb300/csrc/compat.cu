@@ -1,0 +1,576 @@
+// compat.cu -- the reference library's arithmetic on the GB300 pipeline.
+//
+// Compiled with --use_fast_math, the flag the reference builds with
+// (Makefile:26), so expf/powf/sqrtf/division in the filter coefficients map to
+// the same hardware approximations and the per-tap weights agree with the
+// reference's GPU build bit for bit; only the summation order differs.
+//
+// Pipeline per call (all on the caller's stream, no host synchronisation):
+//   k_bin_count / k_scan_tiles / k_bin_scatter  samples -> tile-sorted records
+//   k_grid_compat     one CTA per (tile, resample): taps accumulated in shared
+//                     memory, flushed once with f_hat[c].x += acc[c]
+//   FFT               in-place inverse FFT of ng points with the reference's
+//                     deconvolution fused into the last pass
+//                     (single CTA for ng <= 2^14 (f32) / 2^13 (f64), four-step
+//                     otherwise; non power-of-two ng falls back to cuFFT +
+//                     k_compat_normalize)
+#include <cufft.h>
+#include <limits.h>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <algorithm>
+#include "binning.cuh"
+#include "fft.cuh"
+#include "runtime.h"
+
+namespace cuna {
+namespace {
+
+#define CUNA_PI 3.14159265358979323846
+
+template <typename T> struct FpOf;
+template <> struct FpOf<float> { typedef cuna2_filter_properties_f32 type; };
+template <> struct FpOf<double> { typedef cuna2_filter_properties_f64 type; };
+
+constexpr int kCompatLogTL = 12;  // 4096-cell tiles
+constexpr int kCompatMaxRf = 64;  // shared E3 table size
+
+// ---------------------------------------------------------------------------
+// filter precompute: set_gpu_filter_properties, src/gaussian_filter.cu:204-228
+// ---------------------------------------------------------------------------
+__global__ void k_compat_filter_f32(cuna2_filter_properties_f32 *f, const float *x, int ng, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    int u = (int)(ng * x[i] - f->filter_radius);
+    float eps = ng * x[i] - u;
+    float eps2 = eps / f->b;
+    f->E1[i] = expf(-eps * eps2) / sqrtf(CUNA_PI * f->b);
+    f->E2[i] = expf(2 * eps2);
+  } else if (i < n + f->filter_radius) {
+    int m = i - n;
+    f->E3[m] = expf(-m * m / f->b);
+  }
+}
+
+__global__ void k_compat_filter_f64(cuna2_filter_properties_f64 *f, const double *x, int ng, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    int u = (int)(ng * x[i] - f->filter_radius);
+    double eps = ng * x[i] - u;
+    double eps2 = eps / f->b;
+    f->E1[i] = exp(-eps * eps2) / sqrt(CUNA_PI * f->b);
+    f->E2[i] = exp(2 * eps2);
+  } else if (i < n + f->filter_radius) {
+    int m = i - n;
+    f->E3[m] = exp(-m * m / f->b);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// deconvolution factor of normalize / normalize_bootstrap,
+// src/gaussian_filter.cu:278-302
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float compat_fac(int k, int ng, float b, float normfac) {
+  float K = ((float)k) / ((float)ng);
+  return normfac * expf(K * K * b * 0.25);
+}
+__device__ __forceinline__ double compat_fac(int k, int ng, double b, double normfac) {
+  double K = ((double)k) / ((double)ng);
+  return normfac * exp(K * K * b * 0.25);
+}
+
+__device__ __forceinline__ float cpow(float a, int m) { return powf(a, m); }
+__device__ __forceinline__ double cpow(double a, int m) { return pow(a, m); }
+
+// wang_hash and rand_XORSHIFT, src/gridding.cu:67-82
+__device__ __forceinline__ unsigned wang_hash(unsigned s) {
+  s = (s ^ 61u) ^ (s >> 16);
+  s *= 9u;
+  s = s ^ (s >> 4);
+  s *= 0x27d4eb2du;
+  s = s ^ (s >> 15);
+  return s;
+}
+__device__ __forceinline__ unsigned xorshift32(unsigned s) {
+  s ^= (s << 13);
+  s ^= (s >> 17);
+  s ^= (s << 5);
+  return s;
+}
+
+// Reference cell j = (int)((x + 0.5) * (ng - 1)) (double arithmetic,
+// src/gridding.cu:43,93) and the tap bounds of :53-58.  Returns false when the
+// tap range is empty.  |j| beyond 2^30 is treated as empty: the reference's
+// int arithmetic overflows there and writes out of bounds.
+__device__ __forceinline__ bool compat_taps(double xd, int ng, int rf, bool clamp, int &j, int &ms,
+                                            int &me) {
+  j = (int)((xd + 0.5) * (ng - 1));
+  if (clamp) {
+    if (j >= ng) j = ng - 1;
+    if (j < 0) j = 0;
+  }
+  if (j > (1 << 30) || j < -(1 << 30)) return false;
+  ms = -rf + 1;
+  me = rf;
+  if (j + ms < 0) ms = -j;
+  if (j + me > ng) me = ng - j;
+  return ms < me;
+}
+
+// ---------------------------------------------------------------------------
+// samplers for the binning kernels
+// ---------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ void set_val(RecF &r, float v) { r.p = __float_as_int(v); }
+template <typename T> __device__ __forceinline__ void set_val(RecD &r, double v) { r.v = v; }
+
+template <typename T, bool BOOT> struct SampCompat {
+  typedef typename RecOf<T>::type Rec;
+  typedef typename FpOf<T>::type FP;
+  const T *x;
+  const T *y;
+  const FP *fp;
+  int64_t n;
+  int ng;
+  __device__ __forceinline__ void prep(int64_t i, Prep<Rec> &p) const {
+    int j, ms, me;
+    p.nt = 0;
+    if (!compat_taps((double)x[i], ng, fp->filter_radius, !BOOT, j, ms, me)) return;
+    const int t0 = (j + ms) >> kCompatLogTL, t1 = (j + me - 1) >> kCompatLogTL;
+    p.t[0] = t0;
+    p.t[1] = t1;
+    p.nt = t0 == t1 ? 1 : 2;
+    p.rec.cell = j;
+    if (BOOT) {
+      p.rec.p = (int)i;
+    } else {
+      p.rec.a = fp->E1[i];
+      p.rec.b = fp->E2[i];
+      set_val<T>(p.rec, y ? y[i] : (T)1.0);
+    }
+  }
+};
+
+__device__ __forceinline__ float rec_val(const RecF &r) { return __int_as_float(r.p); }
+__device__ __forceinline__ double rec_val(const RecD &r) { return r.v; }
+
+// ---------------------------------------------------------------------------
+// tiled gridding: fast_gridding / fast_gridding_bootstrap,
+// src/gridding.cu:36-65,86-117
+// ---------------------------------------------------------------------------
+template <typename T, bool BOOT>
+__global__ void __launch_bounds__(256) k_grid_compat(const typename RecOf<T>::type *__restrict__ recs,
+                                                     const int *__restrict__ off,
+                                                     typename CxOf<T>::type *f_hat, int ng,
+                                                     const typename FpOf<T>::type *fp,
+                                                     const T *__restrict__ y, int n, unsigned seed) {
+  typedef typename RecOf<T>::type Rec;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *acc = reinterpret_cast<T *>(smem_raw);
+  T *e3 = acc + (1 << kCompatLogTL);
+  const int tile = blockIdx.x, slab = blockIdx.y;
+  const int base = tile << kCompatLogTL;
+  const int tl = min(1 << kCompatLogTL, ng - base);
+  const int rf = fp->filter_radius;
+  const T *E3g = fp->E3;
+  for (int c = threadIdx.x; c < tl; c += blockDim.x) acc[c] = (T)0;
+  for (int m = threadIdx.x; m < rf && m < kCompatMaxRf; m += blockDim.x) e3[m] = E3g[m];
+  __syncthreads();
+  const T *E1g = fp->E1, *E2g = fp->E2;
+  const int r1 = off[tile + 1];
+  for (int r = off[tile] + threadIdx.x; r < r1; r += blockDim.x) {
+    const Rec rc = recs[r];
+    const int j = rc.cell;
+    int ms = -rf + 1, me = rf;
+    if (j + ms < 0) ms = -j;
+    if (j + me > ng) me = ng - j;
+    T E1, E2, val;
+    if (BOOT) {
+      const int i = slab * n + rc.p;
+      int d = rc.p;
+      val = (T)1.0;
+      if (y) {
+        d = xorshift32(wang_hash(seed + i)) % n;
+        val = y[d];
+      }
+      E1 = E1g[d];
+      E2 = E2g[d];
+    } else {
+      E1 = rc.a;
+      E2 = rc.b;
+      val = rec_val(rc);
+    }
+    const int lo = max(ms, base - j), hi = min(me, base + tl - j);
+    for (int m = lo; m < hi; ++m) {
+      const int mp = m < 0 ? -m : m;
+      const T e3m = mp < kCompatMaxRf ? e3[mp] : E3g[mp];
+      const T w = val * (E1 * cpow(E2, m) * e3m);
+      atomicAdd(&acc[j + m - base], w);
+    }
+  }
+  __syncthreads();
+  typename CxOf<T>::type *out = f_hat + (int64_t)slab * ng + base;
+  for (int c = threadIdx.x; c < tl; c += blockDim.x) {
+    const T v = acc[c];
+    if (v != (T)0) out[c].x += v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FFT with the reference deconvolution fused in
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512) k_fft_single_compat(typename CxOf<T>::type *data, FftDev<T> f,
+                                                            const typename FpOf<T>::type *fp, int norm) {
+  typedef typename CxOf<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *s = reinterpret_cast<C *>(smem_raw);
+  const int L = 1 << f.logL;
+  C *d = data + (int64_t)blockIdx.x * L;
+  for (int i = threadIdx.x; i < L; i += blockDim.x) s[pad16(i)] = d[i];
+  __syncthreads();
+  smem_fft<T>(s, 0, f.logL, 1, f.tw1);
+  const T b = fp->b, nf = fp->normfac;
+  for (int k = threadIdx.x; k < L; k += blockDim.x)
+    d[k] = norm ? cscale(s[pad16(k)], compat_fac(k, L, b, nf)) : s[pad16(k)];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) k_fft_rowpass_compat(const typename CxOf<T>::type *in,
+                                                            typename CxOf<T>::type *out, FftDev<T> f,
+                                                            const typename FpOf<T>::type *fp,
+                                                            int64_t slab_stride, int norm) {
+  typedef typename CxOf<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *s = reinterpret_cast<C *>(smem_raw);
+  const int L2 = 1 << f.logL2;
+  const int logB = ilog2i((int64_t)blockDim.x * kFftE) - f.logL2;
+  const int B = 1 << logB;
+  const int pitch = fft_pitch(L2, B);
+  const int r0 = blockIdx.x * B;
+  const C *src = in + blockIdx.y * slab_stride + (int64_t)r0 * L2;
+  C *dst = out + blockIdx.y * slab_stride;
+  const int tot = B << f.logL2;
+  for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+    const int row = idx >> f.logL2, n2 = idx & (L2 - 1);
+    s[row * pitch + pad16(n2)] = src[idx];
+  }
+  __syncthreads();
+  smem_fft<T>(s, pitch, f.logL2, B, f.tw2);
+  const T b = fp->b, nf = fp->normfac;
+  const int L = 1 << f.logL;
+  for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+    const int k2 = idx >> logB, rl = idx & (B - 1);
+    const int k = r0 + rl + (k2 << f.logL1);
+    const C v = s[rl * pitch + pad16(k2)];
+    dst[k] = norm ? cscale(v, compat_fac(k, L, b, nf)) : v;
+  }
+}
+
+template <typename T>
+__global__ void k_compat_normalize(typename CxOf<T>::type *f_hat, int ng, int64_t total,
+                                   const typename FpOf<T>::type *fp) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < total) f_hat[i] = cscale(f_hat[i], compat_fac((int)(i % ng), ng, fp->b, fp->normfac));
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+template <typename T> FftDev<T> to_dev(const FftGeom &g) {
+  typedef typename CxOf<T>::type C;
+  FftDev<T> f;
+  f.logL = g.logL;
+  f.logL1 = g.logL1;
+  f.logL2 = g.logL2;
+  f.tw1 = (const C *)g.tw1;
+  f.tw2 = (const C *)g.tw2;
+  f.twlo = (const C *)g.twlo;
+  f.twhi = (const C *)g.twhi;
+  return f;
+}
+
+size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// cuFFT comparator plans for non power-of-two grids, cached per
+// (device, stream, ng, batch, precision).
+std::mutex g_cufft_mu;
+std::map<std::tuple<int, cudaStream_t, int, int, int>, cufftHandle> *g_cufft =
+    new std::map<std::tuple<int, cudaStream_t, int, int, int>, cufftHandle>();
+
+template <typename T>
+int cufft_inverse(typename CxOf<T>::type *data, int ng, int nbs, cudaStream_t st) {
+  int dev = 0;
+  CUNA_CK(cudaGetDevice(&dev));
+  cufftHandle h;
+  {
+    std::lock_guard<std::mutex> lk(g_cufft_mu);
+    auto key = std::make_tuple(dev, st, ng, nbs, (int)sizeof(T));
+    auto it = g_cufft->find(key);
+    if (it == g_cufft->end()) {
+      int dims[1] = {ng};
+      cufftResult r = cufftPlanMany(&h, 1, dims, nullptr, 1, ng, nullptr, 1, ng,
+                                    sizeof(T) == 4 ? CUFFT_C2C : CUFFT_Z2Z, nbs);
+      if (r != CUFFT_SUCCESS) return fail(CUNA2_ERROR_CUFFT, "cufftPlanMany failed (%d)", (int)r);
+      if ((r = cufftSetStream(h, st)) != CUFFT_SUCCESS)
+        return fail(CUNA2_ERROR_CUFFT, "cufftSetStream failed (%d)", (int)r);
+      (*g_cufft)[key] = h;
+    } else {
+      h = it->second;
+    }
+  }
+  cufftResult r;
+  if (sizeof(T) == 4)
+    r = cufftExecC2C(h, (cufftComplex *)data, (cufftComplex *)data, CUFFT_INVERSE);
+  else
+    r = cufftExecZ2Z(h, (cufftDoubleComplex *)data, (cufftDoubleComplex *)data, CUFFT_INVERSE);
+  if (r != CUFFT_SUCCESS) return fail(CUNA2_ERROR_CUFFT, "cufftExec failed (%d)", (int)r);
+  return CUNA2_SUCCESS;
+}
+
+template <typename T>
+int compat_normalize(typename CxOf<T>::type *f_hat, int ng, int nbs, const typename FpOf<T>::type *dfp,
+                     cudaStream_t st) {
+  const int64_t total = (int64_t)ng * nbs;
+  if (total == 0) return CUNA2_SUCCESS;
+  k_compat_normalize<T><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(f_hat, ng, total, dfp);
+  CUNA_CK(cudaGetLastError());
+  return CUNA2_SUCCESS;
+}
+
+// In-place inverse FFT of nbs slabs of ng points; `norm` fuses the reference
+// deconvolution into the last pass.
+template <typename T>
+int compat_fft(typename CxOf<T>::type *f_hat, int ng, int nbs, const typename FpOf<T>::type *dfp,
+               typename CxOf<T>::type *scratch, bool norm, cudaStream_t st) {
+  typedef typename CxOf<T>::type C;
+  const bool pow2 = (ng & (ng - 1)) == 0;
+  const int logL = ilog2i(ng);
+  // four-step limit: the column pass holds at least one column of L1 points
+  const int max_log = sizeof(T) == 4 ? 26 : 24;
+  if (!pow2 || logL > max_log) {
+    CUNA_TRY(cufft_inverse<T>(f_hat, ng, nbs, st));
+    return norm ? compat_normalize<T>(f_hat, ng, nbs, dfp, st) : CUNA2_SUCCESS;
+  }
+  FftGeom g;
+  CUNA_TRY(fft_geometry(sizeof(T) == 8, logL, &g));
+  FftDev<T> f = to_dev<T>(g);
+  if (g.single) {
+    const int L = 1 << logL;
+    const int threads = max(32, L / kFftE);
+    const size_t smem = sizeof(C) * (size_t)fft_pitch(L, 1);
+    static bool attr = false;
+    if (!attr) {
+      CUNA_CK(cudaFuncSetAttribute(k_fft_single_compat<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   200 * 1024));
+      attr = true;
+    }
+    k_fft_single_compat<T><<<nbs, threads, smem, st>>>(f_hat, f, dfp, norm ? 1 : 0);
+    CUNA_CK(cudaGetLastError());
+    return CUNA2_SUCCESS;
+  }
+  const int elems = sizeof(T) == 4 ? kPassElemsF32 : kPassElemsF64;
+  const int threads = elems / kFftE;
+  const int L1 = 1 << g.logL1, L2 = 1 << g.logL2;
+  const int BA = elems / L1, BB = elems / L2;
+  const size_t smemA = sizeof(C) * (size_t)BA * fft_pitch(L1, BA);
+  const size_t smemB = sizeof(C) * (size_t)BB * fft_pitch(L2, BB);
+  static bool attr2 = false;
+  if (!attr2) {
+    CUNA_CK(cudaFuncSetAttribute(k_fft_colpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CUNA_CK(cudaFuncSetAttribute(k_fft_rowpass_compat<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 200 * 1024));
+    attr2 = true;
+  }
+  const int64_t L = (int64_t)ng;
+  k_fft_colpass<T><<<dim3(L2 / BA, nbs), threads, smemA, st>>>(f_hat, scratch, f, L);
+  CUNA_CK(cudaGetLastError());
+  k_fft_rowpass_compat<T><<<dim3(L1 / BB, nbs), threads, smemB, st>>>(scratch, f_hat, f, dfp, L,
+                                                                      norm ? 1 : 0);
+  CUNA_CK(cudaGetLastError());
+  return CUNA2_SUCCESS;
+}
+
+struct CompatWs {
+  int *counts, *offsets, *cursor;
+  void *recs;
+  void *scratch;
+};
+
+template <typename T>
+int compat_workspace(int n, int ng, int nbs, bool need_fft, cudaStream_t st, CompatWs *cw) {
+  typedef typename CxOf<T>::type C;
+  typedef typename RecOf<T>::type Rec;
+  const int ntiles = (ng + (1 << kCompatLogTL) - 1) >> kCompatLogTL;
+  const bool pow2 = (ng & (ng - 1)) == 0;
+  const bool fourstep = need_fft && pow2 && ilog2i(ng) > (sizeof(T) == 4 ? kSingleLogF32 : kSingleLogF64) &&
+                        ilog2i(ng) <= (sizeof(T) == 4 ? 26 : 24);
+  const size_t o_off = align_up(sizeof(int) * ntiles), o_cur = o_off + align_up(sizeof(int) * (ntiles + 1));
+  const size_t o_rec = o_cur + align_up(sizeof(int) * ntiles);
+  const size_t o_fft = o_rec + align_up(sizeof(Rec) * 2 * (size_t)(n > 0 ? n : 1));
+  const size_t bytes = o_fft + (fourstep ? sizeof(C) * (size_t)ng * nbs : 0);
+  void *ws = nullptr;
+  CUNA_TRY(stream_workspace(st, bytes, &ws));
+  char *w = (char *)ws;
+  cw->counts = (int *)w;
+  cw->offsets = (int *)(w + o_off);
+  cw->cursor = (int *)(w + o_cur);
+  cw->recs = w + o_rec;
+  cw->scratch = fourstep ? (void *)(w + o_fft) : nullptr;
+  return CUNA2_SUCCESS;
+}
+
+int check_args(int n, int ng, int nbs, const void *x, const void *f_hat, const void *dfp) {
+  if (n < 0 || ng < 1 || nbs < 1 || !f_hat || !dfp || (n > 0 && !x))
+    return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument (n=%d ng=%d nbs=%d)", n, ng, nbs);
+  if ((int64_t)n * nbs > INT_MAX || (int64_t)ng * nbs > ((int64_t)1 << 40))
+    return fail(CUNA2_ERROR_UNSUPPORTED, "n*nbs exceeds the reference's int index range");
+  if (nbs > 65535) return fail(CUNA2_ERROR_UNSUPPORTED, "more than 65535 resamples per call");
+  return CUNA2_SUCCESS;
+}
+
+// Gridding stage: binning + tiled gridding, accumulating into f_hat.
+template <typename T>
+int compat_grid(const T *x, const T *y, typename CxOf<T>::type *f_hat, int n, int ng, int nbs,
+                const typename FpOf<T>::type *dfp, unsigned seed, bool boot, const CompatWs &cw,
+                cudaStream_t st) {
+  typedef typename RecOf<T>::type Rec;
+  if (n == 0) return CUNA2_SUCCESS;
+  const int ntiles = (ng + (1 << kCompatLogTL) - 1) >> kCompatLogTL;
+  Rec *recs = (Rec *)cw.recs;
+  SampCompat<T, false> sp{x, y, dfp, n, ng};
+  SampCompat<T, true> sb{x, y, dfp, n, ng};
+  const int sms = device_sm_count();
+  const size_t smc = ntiles <= kBinSmemTiles ? sizeof(int) * ntiles : 0;
+  const int gcount = (int)std::min<int64_t>((n + 4095) / 4096, 4 * sms);
+  const int gscat = (int)((n + 512 * kScatterItems - 1) / (512 * kScatterItems));
+  CUNA_CK(cudaMemsetAsync(cw.counts, 0, sizeof(int) * ntiles, st));
+  if (boot) k_bin_count<<<gcount, 512, smc, st>>>(sb, cw.counts, ntiles);
+  else k_bin_count<<<gcount, 512, smc, st>>>(sp, cw.counts, ntiles);
+  CUNA_CK(cudaGetLastError());
+  k_scan_tiles<<<1, 1024, 0, st>>>(cw.counts, cw.offsets, cw.cursor, ntiles);
+  CUNA_CK(cudaGetLastError());
+  if (boot) k_bin_scatter<<<gscat, 512, 2 * smc, st>>>(sb, cw.offsets, cw.cursor, recs, ntiles);
+  else k_bin_scatter<<<gscat, 512, 2 * smc, st>>>(sp, cw.offsets, cw.cursor, recs, ntiles);
+  CUNA_CK(cudaGetLastError());
+  const size_t smg = sizeof(T) * ((1 << kCompatLogTL) + kCompatMaxRf);
+  if (boot)
+    k_grid_compat<T, true><<<dim3(ntiles, nbs), 256, smg, st>>>(recs, cw.offsets, f_hat, ng, dfp, y, n, seed);
+  else
+    k_grid_compat<T, false><<<dim3(ntiles, 1), 256, smg, st>>>(recs, cw.offsets, f_hat, ng, dfp, y, n, seed);
+  CUNA_CK(cudaGetLastError());
+  return CUNA2_SUCCESS;
+}
+
+template <typename T>
+int compat_run(const T *x, const T *y, typename CxOf<T>::type *f_hat, int n, int ng, int nbs,
+               const typename FpOf<T>::type *dfp, unsigned seed, bool boot, cudaStream_t st) {
+  typedef typename CxOf<T>::type C;
+  clear_error();
+  CUNA_TRY(check_args(n, ng, boot ? nbs : 1, x, f_hat, dfp));
+  if (!boot) nbs = 1;
+  CompatWs cw;
+  CUNA_TRY(compat_workspace<T>(n, ng, nbs, true, st, &cw));
+  CUNA_TRY(compat_grid<T>(x, y, f_hat, n, ng, nbs, dfp, seed, boot, cw, st));
+  return compat_fft<T>(f_hat, ng, nbs, dfp, (C *)cw.scratch, true, st);
+}
+
+template <typename T, typename FP>
+int compat_filter(const T *x, int n, int ng, FP *h, FP *d, cudaStream_t st) {
+  clear_error();
+  if (n < 1 || ng < 1 || !h || !d || !x)
+    return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument (n=%d ng=%d)", n, ng);
+  const int rf = sizeof(T) == 4 ? 6 : 12;  // FILTER_RADIUS, src/gaussian_filter.cu:29-33
+  // host part of generate_pinned_filter_properties, src/gaussian_filter.cu:54-57
+  T R = ((T)ng) / n;
+  h->b = 2 * R / (2 * R - 1) * (rf / CUNA_PI);
+  h->filter_radius = rf;
+  h->normfac = sqrt(2 * CUNA_PI);
+  CUNA_CK(cudaMemcpyAsync(d, h, sizeof(FP), cudaMemcpyHostToDevice, st));
+  const int nb = (n + rf + 255) / 256;
+  if (sizeof(T) == 4)
+    k_compat_filter_f32<<<nb, 256, 0, st>>>((cuna2_filter_properties_f32 *)d, (const float *)x, ng, n);
+  else
+    k_compat_filter_f64<<<nb, 256, 0, st>>>((cuna2_filter_properties_f64 *)d, (const double *)x, ng, n);
+  CUNA_CK(cudaGetLastError());
+  return CUNA2_SUCCESS;
+}
+
+}  // namespace
+}  // namespace cuna
+
+using namespace cuna;
+
+extern "C" int cuna2_compat_filter_radius(int is_double) { return is_double ? 12 : 6; }
+
+extern "C" int cuna2_compat_filter_f32(const float *x, int n, int ng, cuna2_filter_properties_f32 *h,
+                                       cuna2_filter_properties_f32 *d, cudaStream_t st) {
+  return compat_filter<float>(x, n, ng, h, d, st);
+}
+extern "C" int cuna2_compat_filter_f64(const double *x, int n, int ng, cuna2_filter_properties_f64 *h,
+                                       cuna2_filter_properties_f64 *d, cudaStream_t st) {
+  return compat_filter<double>(x, n, ng, h, d, st);
+}
+extern "C" int cuna2_compat_adjoint_f32(const float *x, const float *y, float2 *f_hat, int n, int ng,
+                                        const cuna2_filter_properties_f32 *d, cudaStream_t st) {
+  return compat_run<float>(x, y, f_hat, n, ng, 1, d, 0u, false, st);
+}
+extern "C" int cuna2_compat_adjoint_f64(const double *x, const double *y, double2 *f_hat, int n, int ng,
+                                        const cuna2_filter_properties_f64 *d, cudaStream_t st) {
+  return compat_run<double>(x, y, f_hat, n, ng, 1, d, 0u, false, st);
+}
+extern "C" int cuna2_compat_bootstrap_f32(const float *x, const float *y, float2 *f_hat, int n, int ng,
+                                          int nbs, const cuna2_filter_properties_f32 *d, unsigned seed,
+                                          cudaStream_t st) {
+  return compat_run<float>(x, y, f_hat, n, ng, nbs, d, seed, true, st);
+}
+extern "C" int cuna2_compat_bootstrap_f64(const double *x, const double *y, double2 *f_hat, int n, int ng,
+                                          int nbs, const cuna2_filter_properties_f64 *d, unsigned seed,
+                                          cudaStream_t st) {
+  return compat_run<double>(x, y, f_hat, n, ng, nbs, d, seed, true, st);
+}
+
+extern "C" int cuna2_compat_grid_f32(const float *x, const float *y, float2 *f_hat, int n, int ng,
+                                     const cuna2_filter_properties_f32 *d, cudaStream_t st) {
+  clear_error();
+  CUNA_TRY(check_args(n, ng, 1, x, f_hat, d));
+  CompatWs cw;
+  CUNA_TRY(compat_workspace<float>(n, ng, 1, false, st, &cw));
+  return compat_grid<float>(x, y, f_hat, n, ng, 1, d, 0u, false, cw, st);
+}
+extern "C" int cuna2_compat_grid_f64(const double *x, const double *y, double2 *f_hat, int n, int ng,
+                                     const cuna2_filter_properties_f64 *d, cudaStream_t st) {
+  clear_error();
+  CUNA_TRY(check_args(n, ng, 1, x, f_hat, d));
+  CompatWs cw;
+  CUNA_TRY(compat_workspace<double>(n, ng, 1, false, st, &cw));
+  return compat_grid<double>(x, y, f_hat, n, ng, 1, d, 0u, false, cw, st);
+}
+extern "C" int cuna2_compat_fft_f32(float2 *f_hat, int ng, int nbatch, const cuna2_filter_properties_f32 *d,
+                                    int normalize, cudaStream_t st) {
+  clear_error();
+  CUNA_TRY(check_args(0, ng, nbatch, nullptr, f_hat, d));
+  CompatWs cw;
+  CUNA_TRY(compat_workspace<float>(0, ng, nbatch, true, st, &cw));
+  return compat_fft<float>(f_hat, ng, nbatch, d, (float2 *)cw.scratch, normalize != 0, st);
+}
+extern "C" int cuna2_compat_fft_f64(double2 *f_hat, int ng, int nbatch, const cuna2_filter_properties_f64 *d,
+                                    int normalize, cudaStream_t st) {
+  clear_error();
+  CUNA_TRY(check_args(0, ng, nbatch, nullptr, f_hat, d));
+  CompatWs cw;
+  CUNA_TRY(compat_workspace<double>(0, ng, nbatch, true, st, &cw));
+  return compat_fft<double>(f_hat, ng, nbatch, d, (double2 *)cw.scratch, normalize != 0, st);
+}
+extern "C" int cuna2_compat_normalize_f32(float2 *f_hat, int ng, int nbatch,
+                                          const cuna2_filter_properties_f32 *d, cudaStream_t st) {
+  clear_error();
+  CUNA_TRY(check_args(0, ng, nbatch, nullptr, f_hat, d));
+  return compat_normalize<float>(f_hat, ng, nbatch, d, st);
+}
+extern "C" int cuna2_compat_normalize_f64(double2 *f_hat, int ng, int nbatch,
+                                          const cuna2_filter_properties_f64 *d, cudaStream_t st) {
+  clear_error();
+  CUNA_TRY(check_args(0, ng, nbatch, nullptr, f_hat, d));
+  return compat_normalize<double>(f_hat, ng, nbatch, d, st);
+}

@@ -1,0 +1,59 @@
+// runtime.h -- host-side runtime shared by the compat and accurate paths:
+// error reporting, per-(device, stream) workspaces, cached FFT twiddle tables,
+// and launch-shape constants.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+#include "../../include/cuna2.h"
+
+namespace cuna {
+
+// Record `status` with a printf-style message for cuna2_last_error(); returns
+// status so call sites can `return fail(...)`.
+int fail(int status, const char *fmt, ...);
+// CUDA error -> CUNA2_ERROR_CUDA with the call text.
+int fail_cuda(cudaError_t e, const char *what);
+void clear_error();
+
+#define CUNA_CK(call)                                   \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return fail_cuda(e_, #call); \
+  } while (0)
+#define CUNA_TRY(expr)           \
+  do {                           \
+    int s_ = (expr);             \
+    if (s_ != CUNA2_SUCCESS) return s_; \
+  } while (0)
+
+// Scratch memory for one (current device, stream): grows on demand, never
+// shrinks, freed at process exit.  Calls on different streams get different
+// buffers, so concurrent streams do not race.  Growing synchronises the device.
+int stream_workspace(cudaStream_t stream, size_t bytes, void **ptr);
+
+// Number of SMs of the current device.
+int device_sm_count();
+
+// FFT geometry for a complex length L = 2^logL.  Single-CTA transforms use
+// logL1 = logL and logL2 = 0.
+struct FftGeom {
+  int logL, logL1, logL2;
+  bool single;
+  const void *tw1, *tw2, *twlo, *twhi;
+};
+// Largest single-CTA length (log2) and the per-CTA element budget of the
+// four-step passes for each precision.
+constexpr int kSingleLogF32 = 14;  // 16384 complex64 = 128 KB + padding
+constexpr int kSingleLogF64 = 13;  // 8192 complex128
+constexpr int kPassElemsF32 = 8192;
+constexpr int kPassElemsF64 = 4096;
+constexpr int kMaxLogL = 26;
+
+// Geometry and device twiddle tables (computed in double precision on the
+// host, rounded once to the element type, cached per device).  `min_rows`
+// forces the row pass to hold at least that many rows (2 for the real-input
+// unpack, which pairs rows k1 and L1-k1).
+int fft_geometry(bool is_double, int logL, FftGeom *g);
+
+}  // namespace cuna

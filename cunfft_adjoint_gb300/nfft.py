@@ -1,0 +1,68 @@
+"""Accurate-mode adjoint NFFT plans (cuna2_plan_* over ctypes).
+
+    plan = AdjointNFFT(nf=2**20, R=4, m=12, dtype=torch.float32)
+    F = plan(t, y, t0, T)     # F[k + nf/2] = sum_j y_j exp(2 pi i k x_j),
+                              # x_j = (t_j - t0)/T - 1/2,  k = -nf/2 .. nf/2-1
+
+t is a float64 CUDA tensor; y has the plan's dtype; F is complex64 (float
+plans) or complex128.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+
+
+class AdjointNFFT:
+    def __init__(self, nf, R=2, m=8, dtype=torch.float32, device=None):
+        if dtype not in (torch.float32, torch.float64):
+            raise TypeError("dtype must be torch.float32 or torch.float64")
+        self.nf, self.R, self.m, self.dtype = int(nf), int(R), int(m), dtype
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.cdtype = torch.complex64 if dtype == torch.float32 else torch.complex128
+        self._h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.core().cuna2_plan_create(ctypes.byref(self._h),
+                                                     _lib.F32 if dtype == torch.float32 else _lib.F64,
+                                                     self.nf, self.R, self.m))
+        ng, tau = ctypes.c_int64(), ctypes.c_double()
+        _lib.check(_lib.core().cuna2_plan_info(self._h, ctypes.byref(ng), ctypes.byref(tau)))
+        self.ng, self.tau = ng.value, tau.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.core().cuna2_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = ctypes.c_void_p()
+
+    def __call__(self, t, y, t0=None, T=None, out=None, stream=None):
+        return self.adjoint(t, y, t0, T, out, stream)
+
+    def adjoint(self, t, y, t0=None, T=None, out=None, stream=None):
+        if t.dtype != torch.float64 or not t.is_cuda:
+            raise TypeError("t must be a float64 CUDA tensor")
+        if y.dtype != self.dtype or not y.is_cuda:
+            raise TypeError("y must be a %s CUDA tensor" % self.dtype)
+        t = t.contiguous()
+        y = y.contiguous()
+        n = t.numel()
+        if y.numel() != n:
+            raise ValueError("t and y differ in length")
+        if t0 is None or T is None:
+            lo, hi = float(t.min()), float(t.max())
+            t0 = lo if t0 is None else t0
+            T = (hi - lo if hi > lo else 1.0) if T is None else T
+        if out is None:
+            out = torch.empty(self.nf, dtype=self.cdtype, device=t.device)
+        s = (stream if stream is not None else torch.cuda.current_stream(t.device)).cuda_stream
+        _lib.check(_lib.core().cuna2_adjoint(self._h, t.data_ptr(), y.data_ptr(), out.data_ptr(), n,
+                                             float(t0), float(T), s or None))
+        return out
+
+    def frequencies(self):
+        """Integer frequency index k of each output bin."""
+        return torch.arange(-self.nf // 2, self.nf // 2, dtype=torch.int64)

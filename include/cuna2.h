@@ -1,0 +1,152 @@
+/* cuna2.h -- extern "C" interface of the GB300 adjoint-NFFT library
+ * (libcuna_gb300.so).  Plain pointers and sizes only; every array argument is
+ * CUDA device memory unless stated otherwise; every function returns a status
+ * code (CUNA2_SUCCESS == 0) instead of exiting the process.
+ *
+ * Two families:
+ *
+ *  - cuna2_compat_*: the reference library's arithmetic (CUNA v1.3), the
+ *    C-ABI form of the reference entry points.  The drop-in libraries
+ *    libcunaf.so / libcunad.so (include/cuna.h) are thin wrappers over these.
+ *
+ *  - cuna2_plan_* / cuna2_adjoint*: accurate mode.  Samples at times t_j with
+ *    values y_j are mapped to x_j = (t_j - t0)/T - 1/2 and the library returns
+ *        F_k = sum_j y_j exp(+2 pi i k x_j),   k = -nf/2 .. nf/2 - 1,
+ *    stored at F[k + nf/2], accurate to about 1e-6 relative (float32 plans)
+ *    against a direct double-precision sum.  The grid-index reduction of t_j
+ *    is done in 64-bit fixed point, so long baselines keep full phase
+ *    accuracy.
+ */
+#ifndef CUNA2_H
+#define CUNA2_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------- */
+/* status                                                                  */
+/* ---------------------------------------------------------------------- */
+enum {
+  CUNA2_SUCCESS = 0,
+  CUNA2_ERROR_INVALID_VALUE = 1, /* bad size, NULL pointer, bad plan       */
+  CUNA2_ERROR_CUDA = 2,          /* a CUDA runtime call failed              */
+  CUNA2_ERROR_UNSUPPORTED = 3,   /* size/configuration this build rejects   */
+  CUNA2_ERROR_ALLOC = 4,         /* device or host allocation failed        */
+  CUNA2_ERROR_CUFFT = 5          /* the cuFFT comparator path failed        */
+};
+
+/* Message for the last failing call made by this thread ("" if none). */
+const char *cuna2_last_error(void);
+/* Name of a status code. */
+const char *cuna2_status_string(int status);
+/* Library version string. */
+const char *cuna2_version(void);
+
+/* ---------------------------------------------------------------------- */
+/* compat mode: the reference library's arithmetic                         */
+/* ---------------------------------------------------------------------- */
+
+/* Same memory layout as the reference's filter_properties
+ * (inc/cuna_typedefs.h:92-108) in its float build (40 bytes) and double build
+ * (48 bytes).  E1/E2 hold n values, E3 holds filter_radius values; all three
+ * are device pointers. */
+typedef struct {
+  float b, normfac;
+  int filter_radius;
+  float *E1, *E2, *E3;
+} cuna2_filter_properties_f32;
+
+typedef struct {
+  double b, normfac;
+  int filter_radius;
+  double *E1, *E2, *E3;
+} cuna2_filter_properties_f64;
+
+/* Fill h_fprops->{b, normfac, filter_radius}, copy *h_fprops to d_fprops and
+ * compute E1/E2/E3 on `stream`.  The caller allocates d_fprops (device) and
+ * the E1 (n), E2 (n), E3 (filter_radius) device arrays whose pointers it
+ * stores in h_fprops.  filter_radius is 6 (f32) or 12 (f64).
+ * Replaces generate_pinned_filter_properties, src/gaussian_filter.cu:43-66. */
+int cuna2_compat_filter_f32(const float *x, int n, int ng,
+                            cuna2_filter_properties_f32 *h_fprops,
+                            cuna2_filter_properties_f32 *d_fprops, cudaStream_t stream);
+int cuna2_compat_filter_f64(const double *x, int n, int ng,
+                            cuna2_filter_properties_f64 *h_fprops,
+                            cuna2_filter_properties_f64 *d_fprops, cudaStream_t stream);
+
+/* Radius the compat filter uses: 6 for float, 12 for double. */
+int cuna2_compat_filter_radius(int is_double);
+
+/* Gridding -> in-place unnormalised inverse FFT -> deconvolution on `stream`.
+ * f_hat (ng complex values) ACCUMULATES the gridded samples, exactly as the
+ * reference: zero it first for a plain transform.  f_data == NULL grids
+ * y_j = 1 (the window function).
+ * Replaces cunfft_adjoint_raw_async, src/cuna_kernel.cu:188-232. */
+int cuna2_compat_adjoint_f32(const float *x, const float *f_data, float2 *f_hat, int n,
+                             int ng, const cuna2_filter_properties_f32 *d_fprops,
+                             cudaStream_t stream);
+int cuna2_compat_adjoint_f64(const double *x, const double *f_data, double2 *f_hat, int n,
+                             int ng, const cuna2_filter_properties_f64 *d_fprops,
+                             cudaStream_t stream);
+
+/* nbs bootstrap resamples into f_hat[nbs][ng] (accumulating), same draw
+ * stream as the reference (wang_hash then xorshift32 of seed + i).
+ * Replaces cunfft_adjoint_raw_async_bootstrap, src/cuna_kernel.cu:236-289. */
+int cuna2_compat_bootstrap_f32(const float *x, const float *f_data, float2 *f_hat, int n,
+                               int ng, int nbs, const cuna2_filter_properties_f32 *d_fprops,
+                               unsigned int seed, cudaStream_t stream);
+int cuna2_compat_bootstrap_f64(const double *x, const double *f_data, double2 *f_hat, int n,
+                               int ng, int nbs, const cuna2_filter_properties_f64 *d_fprops,
+                               unsigned int seed, cudaStream_t stream);
+
+/* The three stages of cuna2_compat_adjoint_* separately (the reference's
+ * performGridding / performFFTs / normalizeResults, src/cuna_kernel.cu:52-117):
+ * gridding only (accumulating), the unnormalised in-place inverse FFT of
+ * nbatch slabs of ng points (normalize != 0 fuses the deconvolution in), and
+ * the deconvolution alone. */
+int cuna2_compat_grid_f32(const float *x, const float *f_data, float2 *f_hat, int n, int ng,
+                          const cuna2_filter_properties_f32 *d_fprops, cudaStream_t stream);
+int cuna2_compat_grid_f64(const double *x, const double *f_data, double2 *f_hat, int n, int ng,
+                          const cuna2_filter_properties_f64 *d_fprops, cudaStream_t stream);
+int cuna2_compat_fft_f32(float2 *f_hat, int ng, int nbatch, const cuna2_filter_properties_f32 *d_fprops,
+                         int normalize, cudaStream_t stream);
+int cuna2_compat_fft_f64(double2 *f_hat, int ng, int nbatch, const cuna2_filter_properties_f64 *d_fprops,
+                         int normalize, cudaStream_t stream);
+int cuna2_compat_normalize_f32(float2 *f_hat, int ng, int nbatch,
+                               const cuna2_filter_properties_f32 *d_fprops, cudaStream_t stream);
+int cuna2_compat_normalize_f64(double2 *f_hat, int ng, int nbatch,
+                               const cuna2_filter_properties_f64 *d_fprops, cudaStream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* accurate mode                                                           */
+/* ---------------------------------------------------------------------- */
+enum { CUNA2_F32 = 0, CUNA2_F64 = 1 };
+
+typedef struct cuna2_plan_st *cuna2_plan;
+
+/* Plan for nf output frequencies (even, >= 2), oversampling R (>= 2) and
+ * Gaussian half-width m (2..16 grid cells) in precision dtype.  The grid has
+ * ng = R * nf cells.  Allocates twiddle tables on the current device. */
+int cuna2_plan_create(cuna2_plan *plan, int dtype, int64_t nf, int R, int m);
+int cuna2_plan_destroy(cuna2_plan plan);
+/* Grid size ng and the kernel variance tau (grid cells^2) the plan uses. */
+int cuna2_plan_info(cuna2_plan plan, int64_t *ng, double *tau);
+
+/* One adjoint NFFT: t (n doubles), y (n floats for CUNA2_F32 plans, doubles
+ * for CUNA2_F64), F (nf complex values of the plan's precision).  t0 and T
+ * define x_j = (t_j - t0)/T - 1/2; values outside [t0, t0 + T) wrap
+ * periodically.  Stream-ordered; the plan's workspace grows on demand (the
+ * first call with a larger n allocates, so make it before any stream
+ * capture). */
+int cuna2_adjoint(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
+                  double t0, double T, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CUNA2_H */

@@ -1,0 +1,126 @@
+"""GPU tests of accurate mode (cuna2_plan_* / cuna2_adjoint) against the FP64
+direct NDFT and the oracle's double-precision restatement.
+
+Bars: float32 plans <= 1e-5 relative L2 against the FP64 NDFT; float64
+plans at the Gaussian kernel's own accuracy (about exp(-pi m sqrt(1-1/R))).
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nfft(native_built):
+    from cunfft_adjoint_gb300 import nfft as N
+    return N
+
+
+def _run(N, t, y, nf, R, m, dtype, t0, T):
+    plan = N.AdjointNFFT(nf, R, m, dtype)
+    td = torch.as_tensor(t, dtype=torch.float64, device="cuda")
+    yd = torch.as_tensor(y, dtype=dtype, device="cuda")
+    F = plan(td, yd, t0, T)
+    torch.cuda.synchronize()
+    return F.cpu().numpy().astype(np.complex128)
+
+
+CASES = [
+    # n, nf, R, m, dtype, tol vs NDFT     (grid ng = R nf; small path if ng <= 2^15 f32 / 2^14 f64)
+    (2000, 1024, 2, 8, torch.float32, 1e-5),
+    (10000, 16384, 2, 8, torch.float32, 1e-5),         # cfg1 shape, fused single-CTA path
+    (3000, 2048, 4, 12, torch.float64, 1e-11),
+    (200_000, 1 << 16, 2, 8, torch.float32, 1e-5),     # four-step path
+    (100_000, 1 << 15, 4, 12, torch.float64, 1e-11),   # four-step, double
+    (200_000, 1 << 18, 2, 10, torch.float32, 1e-5),    # cfg5 shape
+]
+
+
+@pytest.mark.parametrize("n,nf,R,m,dtype,tol", CASES)
+def test_vs_ndft(nfft, oracle_lib, n, nf, R, m, dtype, tol):
+    rng = np.random.default_rng(n + nf)
+    t = np.sort(rng.uniform(0, 500.0, n))
+    y = rng.normal(0, 1, n) + 0.5 * np.sin(2 * np.pi * t / 3.7)
+    y = y.astype(np.float32 if dtype == torch.float32 else np.float64)
+    F = _run(nfft, t, y, nf, R, m, dtype, 0.0, 500.0)
+    k = np.arange(-nf // 2, nf // 2)
+    sel = k if nf <= 4096 else np.sort(rng.choice(k, 512, replace=False))
+    D = oracle_lib.ndft(t, y.astype(np.float64), 0.0, 500.0, sel)
+    assert rel_l2(F[sel + nf // 2], D) < tol
+    # full spectrum against the oracle's restatement of the same algorithm
+    O = oracle_lib.accurate_adjoint(t, y.astype(np.float64), 0.0, 500.0, nf, R, m)
+    assert rel_l2(F, O) < max(tol, 1e-12)
+
+
+def test_cfg2_full_size(nfft, oracle_lib):
+    """N = 1e6 in 10 seasonal windows over 3650 d, Nf = 2^20, R = 4, m = 12,
+    float32 (unsorted input), against the FP64 NDFT on 256 random bins."""
+    rng = np.random.default_rng(2)
+    n, nf = 1_000_000, 1 << 20
+    win = rng.integers(0, 10, n)
+    t = win * 365.0 + rng.uniform(0, 200.0, n)
+    y = (np.sin(2 * np.pi * t / 0.7) + 0.3 * np.sin(2 * np.pi * t / 3.3) + 0.1 * np.sin(2 * np.pi * t / 41)
+         + rng.normal(0, 1, n))
+    F = _run(nfft, t, y.astype(np.float32), nf, 4, 12, torch.float32, 0.0, 3650.0)
+    k = np.sort(rng.choice(np.arange(-nf // 2, nf // 2), 256, replace=False))
+    D = oracle_lib.ndft(t, y.astype(np.float32).astype(np.float64), 0.0, 3650.0, k)
+    assert rel_l2(F[k + nf // 2], D) < 1e-5
+
+
+def test_long_baseline_phase(nfft, oracle_lib):
+    """Julian-date times: t0 = 2.45e6 d; the fixed-point reduction keeps the
+    phase exact where a float32 x would lose it entirely."""
+    rng = np.random.default_rng(5)
+    n, nf = 20000, 1 << 14
+    t = 2450000.0 + np.sort(rng.uniform(0, 3000.0, n))
+    y = rng.normal(0, 1, n).astype(np.float32)
+    F = _run(nfft, t, y, nf, 2, 8, torch.float32, 2450000.0, 3000.0)
+    k = np.arange(-nf // 2, nf // 2, 37)
+    D = oracle_lib.ndft(t, y.astype(np.float64), 2450000.0, 3000.0, k)
+    assert rel_l2(F[k + nf // 2], D) < 1e-5
+
+
+def test_periodic_wrap(nfft):
+    """Shifting every time by a multiple of T leaves F unchanged; samples
+    outside [t0, t0 + T) wrap."""
+    rng = np.random.default_rng(6)
+    n, nf = 5000, 4096
+    t = rng.uniform(0, 10.0, n)
+    y = rng.normal(0, 1, n).astype(np.float32)
+    A = _run(nfft, t, y, nf, 2, 8, torch.float32, 0.0, 10.0)
+    B = _run(nfft, t + 30.0, y, nf, 2, 8, torch.float32, 0.0, 10.0)
+    C = _run(nfft, t - 20.0, y, nf, 2, 8, torch.float32, 0.0, 10.0)
+    assert rel_l2(B, A) < 1e-6 and rel_l2(C, A) < 1e-6
+
+
+def test_linearity_and_hermitian(nfft):
+    rng = np.random.default_rng(7)
+    n, nf = 300_000, 1 << 17
+    t = rng.uniform(0, 100.0, n)
+    y1 = rng.normal(0, 1, n).astype(np.float32)
+    y2 = rng.normal(0, 1, n).astype(np.float32)
+    F1 = _run(nfft, t, y1, nf, 2, 8, torch.float32, 0.0, 100.0)
+    F2 = _run(nfft, t, y2, nf, 2, 8, torch.float32, 0.0, 100.0)
+    F3 = _run(nfft, t, (2 * y1 - 3 * y2).astype(np.float32), nf, 2, 8, torch.float32, 0.0, 100.0)
+    assert rel_l2(F3, 2 * F1 - 3 * F2) < 1e-5
+    K = nf // 2
+    assert rel_l2(F1[K - np.arange(1, K)], np.conj(F1[K + np.arange(1, K)])) < 1e-6
+
+
+def test_empty_and_single(nfft):
+    F = _run(nfft, np.zeros(0), np.zeros(0, np.float32), 1024, 2, 8, torch.float32, 0.0, 1.0)
+    assert np.all(F == 0)
+    F = _run(nfft, np.array([0.25]), np.array([1.0], np.float32), 1024, 2, 8, torch.float32, 0.0, 1.0)
+    k = np.arange(-512, 512)
+    np.testing.assert_allclose(F, np.exp(2j * np.pi * k * (0.25 - 0.5)), atol=2e-6)
+
+
+def test_plan_errors(nfft):
+    from cunfft_adjoint_gb300 import CunaError
+    with pytest.raises(CunaError):
+        nfft.AdjointNFFT(1000, 3, 8)   # R*nf/2 not a power of two
+    with pytest.raises(CunaError):
+        nfft.AdjointNFFT(1024, 2, 40)  # m out of range
