@@ -1,0 +1,393 @@
+"""Benchmark: adjoint NFFTs per second on one GB300 (and N replicas).
+
+Workload (default, `--workload large`): one light curve of N = 1,000,000
+samples in 10 seasonal windows of 200 d over 3650 d, y = three sinusoids
+(periods 0.7, 3.3, 41 d; amplitudes 1, 0.3, 0.1) + N(0, 1) noise, Nf = 2^20
+output frequencies, oversampling R = 4, Gaussian half-width m = 12, float32
+gridding/FFT with the 64-bit fixed-point phase reduction (accurate mode).  A
+step is one adjoint NFFT of one such input set.  16 independent input sets
+(192 MB of t and y) rotate across steps, so the inputs of a step are not in
+the 129 MB L2 from the previous use.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU: the transform of one light curve does not shard; `--gpus N` under
+torchrun runs N independent replicas ("replicas only"), value = the sum.
+
+The reference arm (`--impl reference`) times the reference's pipeline (its
+compat arithmetic: R_f = 6 float filter, non-periodic grid of ng = R*Nf cells,
+unnormalised inverse FFT, deconvolution) as the multi-threaded CPU program of
+the oracle, on the machine's host cores; the reference has no CPU implementation
+of its own and its CUDA sources are not available on the GPU machine.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "adjoint NFFTs/sec & HBM GB/s on 1 GB300 at ≤1e-5 rel err vs FP64 NDFT, batched vs plain"
+UNIT = "NFFT/s"
+
+WORKLOADS = {
+    "large": dict(n=1_000_000, nf=1 << 20, R=4, m=12, T=3650.0,
+                  name="large single-series: N=1e6 in 10 seasonal windows over 3650 d, "
+                       "Nf=2^20, R=4, m=12"),
+    "plain": dict(n=10_000, nf=1 << 14, R=2, m=8, T=1.0,
+                  name="plain single-series: N=1e4 sorted U[0,1), Nf=16384, R=2, m=8"),
+}
+NSETS = 16
+
+
+def make_inputs(wl, seed, nsets):
+    """nsets independent input sets of the workload (seeded)."""
+    rng = np.random.default_rng(seed)
+    n = wl["n"]
+    ts, ys = [], []
+    for _ in range(nsets):
+        if wl is WORKLOADS["large"]:
+            win = rng.integers(0, 10, n)
+            t = win * 365.0 + rng.uniform(0, 200.0, n)
+            y = (np.sin(2 * np.pi * t / 0.7) + 0.3 * np.sin(2 * np.pi * t / 3.3)
+                 + 0.1 * np.sin(2 * np.pi * t / 41.0) + rng.normal(0, 1.0, n))
+        else:
+            t = np.sort(rng.uniform(0, 1.0, n))
+            y = np.sin(2 * np.pi * 137 * t) + rng.normal(0, 0.5, n)
+        ts.append(t)
+        ys.append(y)
+    return ts, ys
+
+
+def ndft_check(t, y, F, nf, T, nbins=64, seed=0):
+    """Relative L2 error of F on `nbins` random bins against a direct FP64 sum
+    (numpy, chunked)."""
+    rng = np.random.default_rng(seed)
+    k = np.sort(rng.choice(np.arange(-nf // 2, nf // 2), nbins, replace=False))
+    x = t / T - 0.5
+    D = np.zeros(nbins, np.complex128)
+    for a in range(0, len(x), 200_000):
+        ph = np.outer(k, x[a:a + 200_000])
+        ph -= np.rint(ph)
+        D += np.exp(2j * np.pi * ph) @ y[a:a + 200_000].astype(np.float64)
+    G = F[k + nf // 2].astype(np.complex128)
+    return float(np.linalg.norm(G - D) / np.linalg.norm(D))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index, interval_ms=50):
+        self.index, self.interval = index, interval_ms
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", str(self.interval)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.15)
+        return self
+
+    def __exit__(self, *a):
+        time.sleep(0.1)
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+        else:
+            self.out = ""
+
+    def summary(self):
+        rows = [l.split(",") for l in self.out.strip().splitlines() if l.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if "Active" in v and "Not" not in v:
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def stage_bytes(n, ng, nf, rec_bytes=16, elem=4):
+    """Algorithmic DRAM bytes per launch of each stage of the accurate path
+    (float32 unless elem=8): every input read once, every output written
+    once.  Records are duplicated for the ~2m/TL samples near tile edges;
+    that factor is ignored (it is < 1%)."""
+    L = ng // 2
+    c = 2 * elem
+    return {
+        "bin_count": 8 * n,                                  # read t
+        "scan_tiles": 0,
+        "bin_scatter": 8 * n + elem * n + rec_bytes * n,     # read t, y; write records
+        "grid": rec_bytes * n + elem * ng,                    # read records; write real grid
+        "fft_colpass": 2 * c * L,                            # read + write the packed grid
+        "fft_rowpass": c * L + c * nf,                       # read packed grid; write F
+        "nfft_small": 8 * n + elem * n + c * nf,
+    }
+
+
+def cpu_baseline(wl, budget_s=20.0):
+    """The reference pipeline on the host cores (oracle CPU program)."""
+    from oracle import oracle
+    n, ng = wl["n"], wl["R"] * wl["nf"]
+    ts, ys = make_inputs(wl, 99, 1)
+    t = ts[0]
+    x = ((t - t.min()) / (t.max() - t.min()) - 0.5).astype(np.float32)
+    y = ys[0].astype(np.float32)
+    p = oracle.CpuPipeline(n, ng)
+    p.run(x, y)  # warm-up (page-in, thread pool)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        p.run(x, y)
+        done += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or done >= 50:
+            break
+    return {"value": done / el, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": "%d transforms of the workload (N=%d, ng=%d, reference compat math, float) "
+                      "by the oracle's multi-threaded CPU pipeline" % (done, n, ng),
+            "seconds": round(el, 3)}
+
+
+def dist_setup(backend):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def reference_arm(args, wl):
+    ws, rank, local = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return
+    from oracle import oracle
+    n, ng = wl["n"], wl["R"] * wl["nf"]
+    ts, ys = make_inputs(wl, 7, 2)
+    xs = [((t - t.min()) / (t.max() - t.min()) - 0.5).astype(np.float32) for t in ts]
+    yv = [y.astype(np.float32) for y in ys]
+    p = oracle.CpuPipeline(n, ng)
+    t_est = time.perf_counter()
+    p.run(xs[0], yv[0])
+    one = time.perf_counter() - t_est
+    for w in range(min(args.warmup, 2)):
+        p.run(xs[w % 2], yv[w % 2])
+    steps = args.steps
+    cap = max(1, int(120.0 / max(one, 1e-6)))
+    timed = min(steps, cap)
+    t0 = time.perf_counter()
+    for s in range(timed):
+        p.run(xs[s % 2], yv[s % 2])
+    el = time.perf_counter() - t0
+    value = timed / el
+    sample = ("%d transforms (N=%d, ng=%d, reference compat math, float) by the oracle's "
+              "multi-threaded CPU pipeline%s" % (timed, n, ng, "" if timed == steps else
+                                                 "; %d of %d requested steps, capped at ~120 s" % (timed, steps)))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": timed, "warmup": args.warmup, "ms_per_step": 1000.0 * el / timed,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": wl["name"], "n": n, "ng": ng, "nf": wl["nf"], "R": wl["R"],
+                       "cache": "two input sets alternate; CPU run"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return reference_arm(args, wl)
+
+    import torch
+    from cunfft_adjoint_gb300 import _lib
+    from cunfft_adjoint_gb300.nfft import AdjointNFFT
+
+    ws, rank, local = dist_setup("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n, nf, R, m, T = wl["n"], wl["nf"], wl["R"], wl["m"], wl["T"]
+    ng = R * nf
+    ts, ys = make_inputs(wl, 1000 + rank, NSETS)
+    td = [torch.as_tensor(t, dtype=torch.float64, device=dev) for t in ts]
+    yd = [torch.as_tensor(y.astype(np.float32), device=dev) for y in ys]
+    Fd = [torch.empty(nf, dtype=torch.complex64, device=dev) for _ in range(4)]
+    plan = AdjointNFFT(nf, R, m, torch.float32, device=dev)
+    L = _lib.core()
+    if not args.no_graph:
+        _lib.check(L.cuna2_plan_set_graph(plan._h, 1))
+    stream = torch.cuda.current_stream(dev)
+
+    def step(s):
+        plan.adjoint(td[s % NSETS], yd[s % NSETS], 0.0, T, out=Fd[s % 4])
+
+    for s in range(max(args.warmup, 3) + NSETS):  # every input set gets its graph before timing
+        step(s)
+    torch.cuda.synchronize()
+    # accuracy of one output against a direct FP64 sum
+    err = ndft_check(ts[0], ys[0].astype(np.float32), plan.adjoint(td[0], yd[0], 0.0, T).cpu().numpy(), nf, T)
+
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for s in range(args.steps):
+            step(s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        tmax = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tmax.item())
+        torch.distributed.barrier()
+    ms_step = ms / args.steps
+    value = ws * args.steps / (ms / 1000.0)
+
+    # per-launch durations (CUDA events between launches on the plan's stream)
+    import ctypes
+    stage_ms = (ctypes.c_float * 16)()
+    names = (ctypes.c_char_p * 16)()
+    nst = ctypes.c_int()
+    acc = {}
+    reps = 10
+    for r in range(reps):
+        s = (r * 5) % NSETS
+        _lib.check(L.cuna2_plan_profile(plan._h, td[s].data_ptr(), yd[s].data_ptr(), Fd[0].data_ptr(), n, 0.0, T,
+                                        stream.cuda_stream or None, stage_ms, names, 16, ctypes.byref(nst)))
+        for i in range(nst.value):
+            acc.setdefault(names[i].decode(), []).append(stage_ms[i])
+    stages = {k: float(np.mean(v)) for k, v in acc.items()}
+    sb = stage_bytes(n, ng, nf)
+    dom = max(stages, key=stages.get)
+    peak, peak_kind = peaks()
+    ach = sb.get(dom, 0) / (stages[dom] * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic_large.json")
+    if os.path.exists(tfile):
+        traffic = json.load(open(tfile)).get(dom)
+    total_bytes = sum(sb[k] for k in stages if k in sb)
+    kernels_per_step = len([k for k in stages if k != "start"])
+
+    # e2e: same transform through the host-buffer C-ABI entry, pinned host arrays
+    th = [torch.as_tensor(t).pin_memory() for t in ts[:4]]
+    yh = [torch.as_tensor(y.astype(np.float32)).pin_memory() for y in ys[:4]]
+    Fh = torch.empty(nf, dtype=torch.complex64).pin_memory()
+    e2e_steps = max(1, min(args.steps, 200))
+
+    def host_step(s):
+        _lib.check(L.cuna2_adjoint_host(plan._h, th[s % 4].data_ptr(), yh[s % 4].data_ptr(), Fh.data_ptr(), n,
+                                        0.0, T, stream.cuda_stream or None))
+
+    for s in range(4):
+        host_step(s)
+    torch.cuda.synchronize()
+    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h0.record(stream)
+    for s in range(e2e_steps):
+        host_step(s)
+    h1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = h0.elapsed_time(h1) / e2e_steps
+
+    # float64 side by side (same workload, double plan)
+    f64 = None
+    if rank == 0:
+        plan64 = AdjointNFFT(nf, R, m, torch.float64, device=dev)
+        if not args.no_graph:
+            _lib.check(L.cuna2_plan_set_graph(plan64._h, 1))
+        yd64 = [torch.as_tensor(y, dtype=torch.float64, device=dev) for y in ys[:4]]
+        F64 = torch.empty(nf, dtype=torch.complex128, device=dev)
+        for s in range(8):
+            plan64.adjoint(td[s % 4], yd64[s % 4], 0.0, T, out=F64)
+        torch.cuda.synchronize()
+        k64 = max(10, min(200, args.steps // 10))
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for s in range(k64):
+            plan64.adjoint(td[s % 4], yd64[s % 4], 0.0, T, out=F64)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = a0.elapsed_time(a1) / k64
+        err64 = ndft_check(ts[0], ys[0], plan64.adjoint(td[0], yd64[0], 0.0, T).cpu().numpy(), nf, T)
+        f64 = {"value": 1000.0 / ms64, "unit": UNIT, "ms_per_step": ms64, "rel_err_vs_fp64_ndft": err64,
+               "steps": k64}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(wl)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": wl["name"], "n": n, "nf": nf, "R": R, "m": m, "ng": ng,
+                       "mode": "accurate (fixed-point phase, float32 gridding+FFT)",
+                       "cache": "inputs larger than L2: %d rotating input sets (%.0f MB of t,y)" %
+                                (NSETS, NSETS * n * 12 / 1e6),
+                       "graph": not args.no_graph, "parallelism": "replicas" if ws > 1 else "single"},
+            "rel_err_vs_fp64_ndft": err,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
+                         "traffic": traffic, "algorithmic_bytes": sb.get(dom, 0)},
+            "stages_ms": stages,
+            "pipeline_gbs": total_bytes / (ms_step * 1e-3) / 1e9,
+            "e2e": {"value": 1000.0 / e2e_ms, "unit": UNIT, "ms_per_step": e2e_ms, "steps": e2e_steps,
+                    "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": nf * 8},
+            "gpu_launches": kernels_per_step * args.steps,
+            "clocks": clk.summary(),
+            "f64": f64,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -24,6 +24,7 @@
 #include <math.h>
 #include <algorithm>
 #include <mutex>
+#include <vector>
 #include "binning.cuh"
 #include "fft.cuh"
 #include "phase.cuh"
@@ -284,6 +285,19 @@ struct cuna2_plan_st {
   std::mutex mu;
   void *ws = nullptr;
   size_t ws_bytes = 0;
+  // device staging for cuna2_adjoint_host
+  void *stage = nullptr;
+  size_t stage_bytes = 0;
+  // CUDA-graph replay of the launch sequence, keyed by the call arguments
+  bool use_graph = false;
+  cudaStream_t cap_stream = nullptr;
+  struct GraphEntry {
+    const void *t, *y, *F;
+    int64_t n;
+    double t0, T;
+    cudaGraphExec_t exec;
+  };
+  std::vector<GraphEntry> graphs;
 };
 
 namespace cuna {
@@ -309,6 +323,8 @@ template <typename T> AccParams<T> make_params(const cuna2_plan_st *p) {
 
 int plan_workspace(cuna2_plan_st *p, size_t bytes, void **ws) {
   if (p->ws_bytes < bytes) {
+    for (auto &g : p->graphs) cudaGraphExecDestroy(g.exec);  // they point at the old workspace
+    p->graphs.clear();
     if (p->ws) {
       CUNA_CK(cudaDeviceSynchronize());
       CUNA_CK(cudaFree(p->ws));
@@ -327,9 +343,22 @@ int plan_workspace(cuna2_plan_st *p, size_t bytes, void **ws) {
   return CUNA2_SUCCESS;
 }
 
+// Optional per-launch event marks (cuna2_plan_profile).
+struct Prof {
+  cudaEvent_t ev[16];
+  const char *name[16];
+  int n = 0;
+};
+inline void mark(Prof *pr, const char *name, cudaStream_t st) {
+  if (pr && pr->n < 16) {
+    pr->name[pr->n] = name;
+    cudaEventRecord(pr->ev[pr->n++], st);
+  }
+}
+
 template <typename T>
 int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>::type *F, int64_t n,
-                double t0, double T_, cudaStream_t st) {
+                double t0, double T_, cudaStream_t st, Prof *pr = nullptr) {
   typedef typename CxOf<T>::type C;
   typedef typename RecOf<T>::type Rec;
   if (n < 0 || (n > 0 && (!t || !y)) || !F || !(T_ > 0) || !std::isfinite(T_) || !std::isfinite(t0))
@@ -347,8 +376,10 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     }
     const size_t smem = sizeof(C) * (size_t)fft_pitch(L, 1) + sizeof(T) * (2 * p->m + 2);
     const int threads = std::max(32, std::min(1024, L / kFftE));
+    mark(pr, "start", st);
     k_nfft_small<T><<<1, threads, smem, st>>>(t, y, n, pm, e, f, F);
     CUNA_CK(cudaGetLastError());
+    mark(pr, "nfft_small", st);
     return CUNA2_SUCCESS;
   }
   const int ntiles = p->ntiles;
@@ -362,6 +393,7 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   int *counts = (int *)(w + o_cnt), *offsets = (int *)(w + o_off), *cursor = (int *)(w + o_cur);
   Rec *recs = (Rec *)(w + o_rec);
   T *grid = (T *)(w + o_grid);
+  mark(pr, "start", st);
   CUNA_CK(cudaMemsetAsync(counts, 0, sizeof(int) * ntiles, st));
   if (n > 0) {
     SampAcc<T> smp{t, y, n, pm, e};
@@ -371,10 +403,13 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     const int gscat = (int)((n + 512 * kScatterItems - 1) / (512 * kScatterItems));
     k_bin_count<<<gcount, 512, smc, st>>>(smp, counts, ntiles);
     CUNA_CK(cudaGetLastError());
+    mark(pr, "bin_count", st);
     k_scan_tiles<<<1, 1024, 0, st>>>(counts, offsets, cursor, ntiles);
     CUNA_CK(cudaGetLastError());
+    mark(pr, "scan_tiles", st);
     k_bin_scatter<<<gscat, 512, 2 * smc, st>>>(smp, offsets, cursor, recs, ntiles);
     CUNA_CK(cudaGetLastError());
+    mark(pr, "bin_scatter", st);
   } else {
     k_scan_tiles<<<1, 1024, 0, st>>>(counts, offsets, cursor, ntiles);
     CUNA_CK(cudaGetLastError());
@@ -382,6 +417,7 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   const size_t smg = sizeof(T) * ((size_t(1) << p->logTL) + 2 * p->m + 2);
   k_grid_acc<T><<<ntiles, 256, smg, st>>>(recs, offsets, grid, e);
   CUNA_CK(cudaGetLastError());
+  mark(pr, "grid", st);
   // packed complex view of the real grid
   C *z = reinterpret_cast<C *>(grid);
   const int elems = sizeof(T) == 4 ? kPassElemsF32 : kPassElemsF64;
@@ -398,9 +434,11 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   }
   k_fft_colpass<T><<<dim3(L2 / BA, 1), threads, smemA, st>>>(z, z, f, (int64_t)L);
   CUNA_CK(cudaGetLastError());
+  mark(pr, "fft_colpass", st);
   const int npairs = L1 / 2 + 1;
   k_fft_rowpass_acc<T><<<(npairs + PB - 1) / PB, threads, smemB, st>>>(z, f, e, F);
   CUNA_CK(cudaGetLastError());
+  mark(pr, "fft_rowpass", st);
   return CUNA2_SUCCESS;
 }
 
@@ -447,7 +485,10 @@ extern "C" int cuna2_plan_create(cuna2_plan *plan, int dtype, int64_t nf, int R,
 extern "C" int cuna2_plan_destroy(cuna2_plan p) {
   clear_error();
   if (!p) return CUNA2_SUCCESS;
+  for (auto &g : p->graphs) cudaGraphExecDestroy(g.exec);
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   if (p->ws) cudaFree(p->ws);
+  if (p->stage) cudaFree(p->stage);
   delete p;
   return CUNA2_SUCCESS;
 }
@@ -460,12 +501,126 @@ extern "C" int cuna2_plan_info(cuna2_plan p, int64_t *ng, double *tau) {
   return CUNA2_SUCCESS;
 }
 
+namespace cuna {
+namespace {
+int run_graph(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0, double T,
+              cudaStream_t st);
+}
+}  // namespace cuna
+
 extern "C" int cuna2_adjoint(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0,
                              double T, cudaStream_t st) {
   clear_error();
   if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
   std::lock_guard<std::mutex> lk(p->mu);
+  if (p->use_graph) return run_graph(p, t, y, F, n, t0, T, st);
   if (p->dtype == CUNA2_F32)
     return adjoint_run<float>(p, t, (const float *)y, (float2 *)F, n, t0, T, st);
   return adjoint_run<double>(p, t, (const double *)y, (double2 *)F, n, t0, T, st);
+}
+
+namespace cuna {
+namespace {
+int run_any(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0, double T,
+            cudaStream_t st, Prof *pr) {
+  if (p->dtype == CUNA2_F32) return adjoint_run<float>(p, t, (const float *)y, (float2 *)F, n, t0, T, st, pr);
+  return adjoint_run<double>(p, t, (const double *)y, (double2 *)F, n, t0, T, st, pr);
+}
+
+// Graph path: capture the launch sequence once per argument set on a private
+// stream, then replay it on the caller's stream.
+int run_graph(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0, double T,
+              cudaStream_t st) {
+  for (auto &g : p->graphs)
+    if (g.t == t && g.y == y && g.F == F && g.n == n && g.t0 == t0 && g.T == T) {
+      CUNA_CK(cudaGraphLaunch(g.exec, st));
+      return CUNA2_SUCCESS;
+    }
+  // run once eagerly: sizes the workspace (allocation is not capturable) and
+  // produces this call's result
+  CUNA_TRY(run_any(p, t, y, F, n, t0, T, st, nullptr));
+  if (!p->cap_stream) CUNA_CK(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking));
+  CUNA_CK(cudaStreamSynchronize(st));
+  CUNA_CK(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
+  int s = run_any(p, t, y, F, n, t0, T, p->cap_stream, nullptr);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(p->cap_stream, &graph);
+  if (s) return s;
+  if (e != cudaSuccess) return fail_cuda(e, "cudaStreamEndCapture");
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail_cuda(e, "cudaGraphInstantiate");
+  if (p->graphs.size() >= 64) {
+    cudaGraphExecDestroy(p->graphs.front().exec);
+    p->graphs.erase(p->graphs.begin());
+  }
+  p->graphs.push_back({t, y, F, n, t0, T, exec});
+  return CUNA2_SUCCESS;
+}
+}  // namespace
+}  // namespace cuna
+
+extern "C" int cuna2_plan_set_graph(cuna2_plan p, int enable) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  std::lock_guard<std::mutex> lk(p->mu);
+  p->use_graph = enable != 0;
+  return CUNA2_SUCCESS;
+}
+
+extern "C" int cuna2_adjoint_host(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0,
+                                  double T, cudaStream_t st) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  if (n < 0 || (n > 0 && (!t || !y)) || !F) return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  const size_t es = p->dtype == CUNA2_F32 ? 4 : 8;
+  const size_t bt = align_up(8 * (size_t)(n > 0 ? n : 1)), by = align_up(es * (size_t)(n > 0 ? n : 1));
+  const size_t bF = 2 * es * (size_t)p->nf;
+  if (p->stage_bytes < bt + by + bF) {
+    if (p->stage) {
+      CUNA_CK(cudaDeviceSynchronize());
+      CUNA_CK(cudaFree(p->stage));
+      p->stage = nullptr;
+      p->stage_bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&p->stage, bt + by + bF);
+    if (e != cudaSuccess) return fail(CUNA2_ERROR_ALLOC, "staging buffers: %s", cudaGetErrorString(e));
+    p->stage_bytes = bt + by + bF;
+  }
+  char *d = (char *)p->stage;
+  double *td = (double *)d;
+  void *yd = d + bt, *Fd = d + bt + by;
+  if (n > 0) {
+    CUNA_CK(cudaMemcpyAsync(td, t, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    CUNA_CK(cudaMemcpyAsync(yd, y, es * (size_t)n, cudaMemcpyHostToDevice, st));
+  }
+  CUNA_TRY(p->use_graph ? run_graph(p, td, yd, Fd, n, t0, T, st) : run_any(p, td, yd, Fd, n, t0, T, st, nullptr));
+  CUNA_CK(cudaMemcpyAsync(F, Fd, bF, cudaMemcpyDeviceToHost, st));
+  CUNA_CK(cudaStreamSynchronize(st));
+  return CUNA2_SUCCESS;
+}
+
+extern "C" int cuna2_plan_profile(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0,
+                                  double T, cudaStream_t st, float *stage_ms, const char **stage_names,
+                                  int max_stages, int *nstages) {
+  clear_error();
+  if (!p || !stage_ms || !nstages) return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  Prof pr;
+  for (int i = 0; i < 16; ++i) CUNA_CK(cudaEventCreate(&pr.ev[i]));
+  int s = run_any(p, t, y, F, n, t0, T, st, &pr);
+  if (!s) {
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s = fail_cuda(e, "cudaStreamSynchronize");
+  }
+  int k = 0;
+  for (int i = 1; !s && i < pr.n && k < max_stages; ++i, ++k) {
+    cudaEventElapsedTime(&stage_ms[k], pr.ev[i - 1], pr.ev[i]);
+    if (stage_names) stage_names[k] = pr.name[i];
+  }
+  *nstages = k;
+  for (int i = 0; i < 16; ++i) cudaEventDestroy(pr.ev[i]);
+  return s;
 }

@@ -146,6 +146,26 @@ int cuna2_plan_info(cuna2_plan plan, int64_t *ng, double *tau);
 int cuna2_adjoint(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
                   double t0, double T, cudaStream_t stream);
 
+/* Same transform with HOST arrays (pinned or pageable): copies t and y to
+ * plan-owned device staging buffers, runs on `stream`, copies F back and
+ * synchronises the stream before returning. */
+int cuna2_adjoint_host(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
+                       double t0, double T, cudaStream_t stream);
+
+/* enable != 0: cuna2_adjoint / cuna2_adjoint_host capture their launch
+ * sequence into a CUDA graph the first time they see an argument set
+ * (pointers, n, t0, T) and replay it afterwards (up to 8 cached sets).  The
+ * capture is taken on a private stream; the caller's stream only sees graph
+ * launches. */
+int cuna2_plan_set_graph(cuna2_plan plan, int enable);
+
+/* Run one transform with CUDA events between its launches and return the
+ * duration of each launch in milliseconds (stage_ms[0..*nstages)) and, if
+ * stage_names is non-NULL, a static name for each.  Synchronises `stream`. */
+int cuna2_plan_profile(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
+                       double t0, double T, cudaStream_t stream, float *stage_ms,
+                       const char **stage_names, int max_stages, int *nstages);
+
 #ifdef __cplusplus
 }
 #endif

@@ -81,9 +81,10 @@ def test_adjoint_async_stream(cuna, case):
     n, ng = len(case["x"]), int(case["ng"])
     s = torch.cuda.Stream()
     fp = cuna.FilterProperties(n, x.dtype, x.device)
+    f0 = case.get("f_hat0")
     with torch.cuda.stream(s):
         cuna.generate_pinned_filter_properties(x, n, ng, fp, s)
-        f_hat = torch.zeros(ng, dtype=_ctype(dt), device="cuda")
+        f_hat = _dev(f0) if f0 is not None else torch.zeros(ng, dtype=_ctype(dt), device="cuda")
         cuna.cunfft_adjoint_raw_async(x, y, f_hat, n, ng, fp, s)
     s.synchronize()
     assert rel_l2(f_hat.cpu().numpy(), case["F"]) < (_tol(dt) if _pow2(ng) else 5e-5)
