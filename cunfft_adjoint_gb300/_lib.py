@@ -59,6 +59,7 @@ CORE_SIGNATURES = {
     "cuna2_compat_fft_f64": (_I, [_P, _I, _I, _P, _I, _P]),
     "cuna2_compat_normalize_f32": (_I, [_P, _I, _I, _P, _P]),
     "cuna2_compat_normalize_f64": (_I, [_P, _I, _I, _P, _P]),
+    "cuna2_compat_adjoint_noalloc_f32": (_I, [_P, _P, _P, _I, _I, _P, _P]),
     "cuna2_plan_create": (_I, [_P, _I, _I64, _I, _I]),
     "cuna2_plan_destroy": (_I, [_P]),
     "cuna2_plan_info": (_I, [_P, _P, _P]),

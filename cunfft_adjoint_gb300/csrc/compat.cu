@@ -574,3 +574,187 @@ extern "C" int cuna2_compat_normalize_f64(double2 *f_hat, int ng, int nbatch,
   CUNA_TRY(check_args(0, ng, nbatch, nullptr, f_hat, d));
   return compat_normalize<double>(f_hat, ng, nbatch, d, st);
 }
+
+// ---------------------------------------------------------------------------
+// cuna2_compat_adjoint_noalloc_f32: cuna2_compat_adjoint_f32 for callers that
+// cannot allocate device memory.
+//
+// Everything the transform needs beyond the caller's x, y, f_hat and filter
+// lives in one statically sized device array that the library carries (every
+// GPU that loads the library holds it until the process exits): the tile
+// counters, the sorted sample records, the FFT scratch slab and the twiddle
+// tables.  The entry point therefore never calls cudaMalloc / cudaFree or
+// cuFFT.  Limits: n <= kNoAllocMaxN samples and a power-of-two grid of at
+// most 2^kNoAllocMaxLogNg cells.
+//
+// The first call on a device sets that device up: it looks up the array's
+// device address with cudaGetSymbolAddress (host code may not use the symbol
+// itself as a pointer), fills the twiddle tables with a kernel and
+// synchronises the caller's stream.  Make that first call before any stream
+// capture.  All calls share the one array, which keeps the previous call's
+// contents; the tile counters are cleared at the start of every call.  Calls
+// that overlap on the GPU (different streams, or different host threads)
+// race on the array: serialise them.
+// ---------------------------------------------------------------------------
+namespace cuna {
+namespace {
+constexpr int kNoAllocMaxN = 131072;
+constexpr int kNoAllocMaxLogNg = 17;
+constexpr size_t kNoAllocOffCounts = 0, kNoAllocOffOffsets = 256, kNoAllocOffCursor = 512;
+constexpr size_t kNoAllocOffRecs = 1024;
+constexpr size_t kNoAllocOffFft = kNoAllocOffRecs + sizeof(RecF) * 2 * (size_t)kNoAllocMaxN;
+constexpr size_t kNoAllocOffTw = kNoAllocOffFft + sizeof(float2) * ((size_t)1 << kNoAllocMaxLogNg);
+constexpr size_t kNoAllocTwEntries = 48 * 1024;  // all tables for logL = 0..17 (about 41K entries)
+constexpr size_t kNoAllocBytes = kNoAllocOffTw + sizeof(float2) * kNoAllocTwEntries;
+constexpr int kNoAllocMaxDevices = 64;
+}  // namespace
+}  // namespace cuna
+
+static __device__ __align__(256) unsigned char cuna_noalloc_scratch[cuna::kNoAllocBytes];
+
+namespace cuna {
+namespace {
+
+// exp(+2 pi i (q * step mod denom) / denom) for q < count, evaluated in double
+__global__ void k_noalloc_twiddles(float2 *dst, int count, int step, int denom) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < count) {
+    const long long num = ((long long)q * step) % denom;
+    double s, c;
+    sincospi(2.0 * (double)num / (double)denom, &s, &c);
+    dst[q] = make_float2((float)c, (float)s);
+  }
+}
+
+struct NoAllocDev {
+  bool ready = false;
+  unsigned char *base = nullptr;
+  int sms = 1;
+  FftDev<float> tab[kNoAllocMaxLogNg + 1];
+};
+std::mutex g_noalloc_mu;
+NoAllocDev g_noalloc[kNoAllocMaxDevices];
+
+int noalloc_table(float2 *tw, size_t &used, int count, int step, int denom, const float2 **out,
+                  cudaStream_t st) {
+  if (used + (size_t)count > kNoAllocTwEntries) return fail(CUNA2_ERROR_UNSUPPORTED, "twiddle region too small");
+  float2 *dst = tw + used;
+  k_noalloc_twiddles<<<(count + 255) / 256, 256, 0, st>>>(dst, count, step, denom);
+  CUNA_CK(cudaGetLastError());
+  used += (size_t)count;
+  *out = dst;
+  return CUNA2_SUCCESS;
+}
+
+// Once per device: device address of the array, twiddle tables, SM count.
+int noalloc_setup(int dev, cudaStream_t st, NoAllocDev **out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  NoAllocDev &d = g_noalloc[dev];
+  if (!d.ready) {
+    void *p = nullptr;
+    CUNA_CK(cudaGetSymbolAddress(&p, cuna_noalloc_scratch));
+    d.base = (unsigned char *)p;
+    CUNA_CK(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
+    float2 *tw = (float2 *)(d.base + kNoAllocOffTw);
+    size_t used = 0;
+    for (int logL = 0; logL <= kNoAllocMaxLogNg; ++logL) {
+      FftDev<float> &f = d.tab[logL];
+      const int L = 1 << logL;
+      f.logL = logL;
+      if (logL <= kSingleLogF32) {
+        f.logL1 = logL;
+        f.logL2 = 0;
+      } else {
+        f.logL1 = (logL + 1) / 2;
+        f.logL2 = logL / 2;
+      }
+      const int L1 = 1 << f.logL1, L2 = 1 << f.logL2, nlo = L < 2048 ? L : 2048;
+      CUNA_TRY(noalloc_table(tw, used, L1, 1, L1, &f.tw1, st));
+      CUNA_TRY(noalloc_table(tw, used, L2, 1, L2, &f.tw2, st));
+      if (logL > kSingleLogF32) {
+        CUNA_TRY(noalloc_table(tw, used, nlo, 1, L, &f.twlo, st));
+        CUNA_TRY(noalloc_table(tw, used, L / nlo, nlo, L, &f.twhi, st));
+      } else {
+        f.twlo = f.tw1;
+        f.twhi = f.tw1;
+      }
+    }
+    CUNA_CK(cudaFuncSetAttribute(k_fft_single_compat<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 200 * 1024));
+    CUNA_CK(cudaFuncSetAttribute(k_fft_colpass<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CUNA_CK(cudaFuncSetAttribute(k_fft_rowpass_compat<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 200 * 1024));
+    CUNA_CK(cudaStreamSynchronize(st));
+    d.ready = true;
+  }
+  *out = &d;
+  return CUNA2_SUCCESS;
+}
+
+int compat_adjoint_noalloc(const float *x, const float *y, float2 *f_hat, int n, int ng,
+                           const cuna2_filter_properties_f32 *dfp, cudaStream_t st) {
+  clear_error();
+  CUNA_TRY(check_args(n, ng, 1, x, f_hat, dfp));
+  if (n > kNoAllocMaxN)
+    return fail(CUNA2_ERROR_UNSUPPORTED, "no-allocation entry point: n = %d exceeds its maximum of %d samples",
+                n, kNoAllocMaxN);
+  if ((ng & (ng - 1)) != 0 || ilog2i(ng) > kNoAllocMaxLogNg)
+    return fail(CUNA2_ERROR_UNSUPPORTED,
+                "no-allocation entry point: ng = %d must be a power of two of at most %d", ng,
+                1 << kNoAllocMaxLogNg);
+  int dev = 0;
+  CUNA_CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(CUNA2_ERROR_UNSUPPORTED, "device index %d", dev);
+  NoAllocDev *d = nullptr;
+  CUNA_TRY(noalloc_setup(dev, st, &d));
+  int *counts = (int *)(d->base + kNoAllocOffCounts);
+  int *offsets = (int *)(d->base + kNoAllocOffOffsets);
+  int *cursor = (int *)(d->base + kNoAllocOffCursor);
+  RecF *recs = (RecF *)(d->base + kNoAllocOffRecs);
+  float2 *scratch = (float2 *)(d->base + kNoAllocOffFft);
+  const int ntiles = (ng + (1 << kCompatLogTL) - 1) >> kCompatLogTL;
+  // the counters must start at zero; the rest is fully rewritten below
+  CUNA_CK(cudaMemsetAsync(counts, 0, sizeof(int) * ntiles, st));
+  if (n > 0) {
+    SampCompat<float, false> sp{x, y, dfp, n, ng};
+    const size_t smc = sizeof(int) * ntiles;
+    const int gcount = (int)std::min<int64_t>((n + 4095) / 4096, 4 * d->sms);
+    const int gscat = (int)((n + 512 * kScatterItems - 1) / (512 * kScatterItems));
+    k_bin_count<<<gcount, 512, smc, st>>>(sp, counts, ntiles);
+    CUNA_CK(cudaGetLastError());
+    k_scan_tiles<<<1, 1024, 0, st>>>(counts, offsets, cursor, ntiles);
+    CUNA_CK(cudaGetLastError());
+    k_bin_scatter<<<gscat, 512, 2 * smc, st>>>(sp, offsets, cursor, recs, ntiles);
+    CUNA_CK(cudaGetLastError());
+    const size_t smg = sizeof(float) * ((1 << kCompatLogTL) + kCompatMaxRf);
+    k_grid_compat<float, false><<<dim3(ntiles, 1), 256, smg, st>>>(recs, offsets, f_hat, ng, dfp, y, n, 0u);
+    CUNA_CK(cudaGetLastError());
+  }
+  const int logL = ilog2i(ng);
+  const FftDev<float> &f = d->tab[logL];
+  if (logL <= kSingleLogF32) {
+    const int threads = std::max(32, ng / kFftE);
+    const size_t smem = sizeof(float2) * (size_t)fft_pitch(ng, 1);
+    k_fft_single_compat<float><<<1, threads, smem, st>>>(f_hat, f, dfp, 1);
+    CUNA_CK(cudaGetLastError());
+    return CUNA2_SUCCESS;
+  }
+  const int threads = kPassElemsF32 / kFftE;
+  const int L1 = 1 << f.logL1, L2 = 1 << f.logL2;
+  const int BA = kPassElemsF32 / L1, BB = kPassElemsF32 / L2;
+  const size_t smemA = sizeof(float2) * (size_t)BA * fft_pitch(L1, BA);
+  const size_t smemB = sizeof(float2) * (size_t)BB * fft_pitch(L2, BB);
+  k_fft_colpass<float><<<dim3(L2 / BA, 1), threads, smemA, st>>>(f_hat, scratch, f, (int64_t)ng);
+  CUNA_CK(cudaGetLastError());
+  k_fft_rowpass_compat<float><<<dim3(L1 / BB, 1), threads, smemB, st>>>(scratch, f_hat, f, dfp, (int64_t)ng, 1);
+  CUNA_CK(cudaGetLastError());
+  return CUNA2_SUCCESS;
+}
+
+}  // namespace
+}  // namespace cuna
+
+extern "C" int cuna2_compat_adjoint_noalloc_f32(const float *x, const float *y, float2 *f_hat, int n, int ng,
+                                                const cuna2_filter_properties_f32 *d, cudaStream_t st) {
+  return compat_adjoint_noalloc(x, y, f_hat, n, ng, d, st);
+}

@@ -122,6 +122,30 @@ int cuna2_compat_normalize_f32(float2 *f_hat, int ng, int nbatch,
 int cuna2_compat_normalize_f64(double2 *f_hat, int ng, int nbatch,
                                const cuna2_filter_properties_f64 *d_fprops, cudaStream_t stream);
 
+/* cuna2_compat_adjoint_f32 for callers that cannot allocate device memory.
+ * No counterpart in the reference library.
+ *
+ * Some callers must not call cudaMalloc once they are running: real-time or
+ * latency-critical loops (cudaFree synchronises the whole device), processes
+ * whose device memory belongs to a framework's caching allocator, and plugin
+ * hosts whose contract forbids a plugin from allocating.  This entry point
+ * allocates nothing: its scratch (tile counters, sorted sample records, FFT
+ * scratch, twiddle tables) is one statically sized device array of about
+ * 5.6 MB that every GPU loading the library holds until the process exits.
+ * The caller still passes x, f_data, f_hat and d_fprops, with the same
+ * meaning as cuna2_compat_adjoint_f32.
+ *
+ * Limits: n <= 131072 samples; ng a power of two <= 131072.  Larger sizes
+ * return CUNA2_ERROR_UNSUPPORTED with a message and touch nothing.
+ * The first call on a device sets it up (looks up the array's device address,
+ * fills the twiddle tables, synchronises `stream`): make it before any stream
+ * capture.  Every call shares the array and keeps the previous call's
+ * contents; the counters are cleared per call.  Calls that overlap on the GPU
+ * race on the array, so serialise them. */
+int cuna2_compat_adjoint_noalloc_f32(const float *x, const float *f_data, float2 *f_hat, int n,
+                                     int ng, const cuna2_filter_properties_f32 *d_fprops,
+                                     cudaStream_t stream);
+
 /* ---------------------------------------------------------------------- */
 /* accurate mode                                                           */
 /* ---------------------------------------------------------------------- */
