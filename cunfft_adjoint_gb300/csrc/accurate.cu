@@ -61,8 +61,14 @@ __device__ __forceinline__ double frac_of(uint64_t lo, double) {
 template <typename T>
 __device__ __forceinline__ void reduce_sample(double t, const PhaseMul &pm, int64_t ng, int &cell, T &f) {
   const uint64_t S = phase_of(t, pm);
-  cell = (int)umulhi64(S, (uint64_t)ng);
-  f = frac_of(S * (uint64_t)ng, (T)0);
+  if ((ng & (ng - 1)) == 0) {  // ng = 2^g: the top g bits are the cell
+    const int g = 63 - __clzll((long long)ng);
+    cell = g ? (int)(S >> (64 - g)) : 0;
+    f = frac_of(S << g, (T)0);
+  } else {
+    cell = (int)umulhi64(S, (uint64_t)ng);
+    f = frac_of(S * (uint64_t)ng, (T)0);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -139,26 +145,35 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512) k_nfft_small(cons
 // ---------------------------------------------------------------------------
 // binning sampler, tiled gridding, last FFT pass
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void rec_set(RecF &r, int cell, float a, float b, float binv) {
-  r.cell = cell; r.a = a; r.b = b; r.p = __float_as_int(binv);
+// Sorted sample record of accurate mode: {cell, fractional cell, value}.
+__device__ __forceinline__ void rec_set(RecF &r, int cell, float fr, float y) {
+  r.cell = cell; r.a = fr; r.b = y; r.p = 0;
 }
-__device__ __forceinline__ void rec_set(RecD &r, int cell, double a, double b, double binv) {
-  r.cell = cell; r.p = 0; r.a = a; r.b = b; r.v = binv;
+__device__ __forceinline__ void rec_set(RecD &r, int cell, double fr, double y) {
+  r.cell = cell; r.p = 0; r.a = fr; r.b = y; r.v = 0.0;
 }
-__device__ __forceinline__ float rec_binv(const RecF &r) { return __int_as_float(r.p); }
-__device__ __forceinline__ double rec_binv(const RecD &r) { return r.v; }
 
 template <typename T> struct SampAcc {
   typedef typename RecOf<T>::type Rec;
+  struct Raw {
+    double t;
+    T y;
+  };
   const double *t;
   const T *y;
   int64_t n;
   PhaseMul pm;
   AccParams<T> e;
-  __device__ __forceinline__ void prep(int64_t i, Prep<Rec> &p) const {
+  __device__ __forceinline__ Raw load(int64_t i, bool with_value) const {
+    Raw r;
+    r.t = t[i];
+    if (with_value) r.y = y[i];
+    return r;
+  }
+  __device__ __forceinline__ void prep(int64_t i, const Raw &r, Prep<Rec> &p) const {
     int cell;
     T fr;
-    reduce_sample<T>(t[i], pm, e.ng, cell, fr);
+    reduce_sample<T>(r.t, pm, e.ng, cell, fr);
     const int ng = (int)e.ng;
     int lo = cell - e.m + 1, hi = cell + e.m;
     if (lo < 0) lo += ng;
@@ -167,56 +182,190 @@ template <typename T> struct SampAcc {
     p.t[0] = t0;
     p.t[1] = t1;
     p.nt = t0 == t1 ? 1 : 2;
-    const T E1 = exp2_t(-e.k1 * fr * fr), E2 = exp2_t(e.k2 * fr);
-    rec_set(p.rec, cell, y[i] * E1, E2, (T)1 / E2);
+    rec_set(p.rec, cell, fr, r.y);
   }
 };
 
+// ---------------------------------------------------------------------------
+// Gridding, gather form.  One CTA owns tile [base, base + TL) of the grid and
+// the records binned to it (its own samples plus the halo samples within m
+// cells of its edges).  Per chunk of at most CAP records it counting-sorts
+// them in shared memory by local slot lc = cell - base + m (integer atomics
+// only), then every thread sums, for each of its cells c, the samples whose
+// slot lies in [c - base, c - base + 2m): w = y exp(-(d - f)^2 / (4 tau)),
+// d = c - cell.  Partial sums stay in registers across chunks and are written
+// once, coalesced.  No floating-point atomics.
+// ---------------------------------------------------------------------------
+template <typename T> struct GridCfg;
+template <> struct GridCfg<float> { static constexpr int CAP = 1024; };
+template <> struct GridCfg<double> { static constexpr int CAP = 512; };
+constexpr int kGridThreads = 256;
+constexpr int kGridMaxCpt = 16;  // cells per thread: TL <= 4096
+
+// 2^x with the hardware approximation (relative error < 2^-22 over the range
+// used here; arguments are <= 0 and results below 2^-126 flush to zero, far
+// beneath the 1e-6 accuracy of the float path).
+__device__ __forceinline__ float ex2_fast(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float gauss_w(float y, float dd, float k1) { return y * ex2_fast(-k1 * dd * dd); }
+__device__ __forceinline__ double gauss_w(double y, double dd, double k1) { return y * exp2(-k1 * dd * dd); }
+
+template <typename T> struct Pair;
+template <> struct Pair<float> { typedef float2 type; };
+template <> struct Pair<double> { typedef double2 type; };
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_grid_acc(const typename RecOf<T>::type *__restrict__ recs,
-                                                  const int *__restrict__ off, T *__restrict__ grid,
-                                                  AccParams<T> e) {
+__global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 4 : 2) k_grid_acc(const typename RecOf<T>::type *__restrict__ recs,
+                                                           const int *__restrict__ off, T *__restrict__ grid,
+                                                           AccParams<T> e) {
   typedef typename RecOf<T>::type Rec;
+  constexpr int CAP = GridCfg<T>::CAP;
+  constexpr int RPT = CAP / kGridThreads;  // records per thread per chunk
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int TL = 1 << e.logTL;
-  T *acc = reinterpret_cast<T *>(smem_raw);
-  T *e3 = acc + TL;
-  const int m = e.m, ng = (int)e.ng;
+  const int TL = 1 << e.logTL, m = e.m, W = TL + 2 * m;
+  const int ng = (int)e.ng;
+  typedef typename Pair<T>::type P2;
+  int *start = reinterpret_cast<int *>(smem_raw);                 // W + 1 slots
+  P2 *sfy = reinterpret_cast<P2 *>(smem_raw + sizeof(int) * ((W + 2 + 3) & ~3));  // (frac, y)
+  short *slc = reinterpret_cast<short *>(sfy + CAP);
+  // a single tile spanning the whole grid maps a record to up to two slots;
+  // halve the chunk then so that placements never exceed CAP
+  const int chunk = (TL + 2 * m > ng) ? CAP / 2 : CAP;
+  __shared__ int wsum[kGridThreads / 32];
   const int tile = blockIdx.x, base = tile << e.logTL;
-  for (int c = threadIdx.x; c < TL; c += blockDim.x) acc[c] = (T)0;
-  for (int d = threadIdx.x; d <= 2 * m; d += blockDim.x) e3[d] = exp_t(e.e3c * (T)((d - m) * (d - m)));
-  __syncthreads();
-  const int r1 = off[tile + 1];
-  for (int r = off[tile] + threadIdx.x; r < r1; r += blockDim.x) {
-    const Rec rc = recs[r];
-    const int c0 = rc.cell;
-    const T E2 = rc.b, E2i = rec_binv(rc);
-    T w = rc.a;
-    for (int d = 0; d <= m; ++d) {
-      int c = c0 + d;
-      if (c >= ng) c -= ng;
-      const int l = c - base;
-      if ((unsigned)l < (unsigned)TL) atomicAdd(&acc[l], w * e3[d + m]);
-      w *= E2;
+  const int cpt = (TL + kGridThreads - 1) / kGridThreads;
+  T acc[kGridMaxCpt];
+#pragma unroll
+  for (int q = 0; q < kGridMaxCpt; ++q) acc[q] = (T)0;
+  const int r0 = off[tile], r1 = off[tile + 1];
+  for (int c0 = r0; c0 < r1; c0 += chunk) {
+    const int cnt = min(chunk, r1 - c0);
+    for (int i = threadIdx.x; i <= W; i += kGridThreads) start[i] = 0;
+    __syncthreads();
+    // load this thread's records; each maps to up to two slots (two only when
+    // the tile wraps onto itself, i.e. a single tile spans the whole grid)
+    Rec rc[RPT];
+    int sl[RPT][2];
+#pragma unroll
+    for (int u = 0; u < RPT; ++u) {
+      const int i = threadIdx.x + u * kGridThreads;
+      if (i < cnt) rc[u] = recs[c0 + i];
     }
-    w = rc.a * E2i;
-    for (int d = -1; d > -m; --d) {
-      int c = c0 + d;
-      if (c < 0) c += ng;
-      const int l = c - base;
-      if ((unsigned)l < (unsigned)TL) atomicAdd(&acc[l], w * e3[d + m]);
-      w *= E2i;
+#pragma unroll
+    for (int u = 0; u < RPT; ++u) {
+      const int i = threadIdx.x + u * kGridThreads;
+      sl[u][0] = sl[u][1] = -1;
+      if (i < cnt) {
+        int p0 = rc[u].cell - base;
+        if (p0 < 0) p0 += ng;
+        // slots p + m for every p = p0 + j*ng in [-m, TL + m), j in {-1, 0, 1}
+        const int a = p0 - ng >= -m ? p0 - ng + m : -1;
+        const int b = p0 < TL + m ? p0 + m : -1;
+        const int c = p0 + ng < TL + m ? p0 + ng + m : -1;
+        sl[u][0] = a >= 0 ? a : (b >= 0 ? b : c);
+        sl[u][1] = a >= 0 ? (b >= 0 ? b : c) : (b >= 0 ? c : -1);
+        if (sl[u][0] >= 0) atomicAdd(&start[sl[u][0]], 1);
+        if (sl[u][1] >= 0) atomicAdd(&start[sl[u][1]], 1);
+      }
     }
+    __syncthreads();
+    // exclusive scan of start[0..W]: slot lc occupies [start[lc], start[lc+1])
+    {
+      const int per = (W + 1 + kGridThreads - 1) / kGridThreads;
+      const int b0 = min(threadIdx.x * per, W + 1), b1 = min(b0 + per, W + 1);
+      int sum = 0;
+      for (int i = b0; i < b1; ++i) sum += start[i];
+      const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+      int v = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+      }
+      if (lane == 31) wsum[w] = v;
+      __syncthreads();
+      if (w == 0) {
+        int t = lane < kGridThreads / 32 ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < kGridThreads / 32; o <<= 1) {
+          const int u2 = __shfl_up_sync(0xffffffffu, t, o);
+          if (lane >= o) t += u2;
+        }
+        if (lane < kGridThreads / 32) wsum[lane] = t;
+      }
+      __syncthreads();
+      int run = v - sum + (w > 0 ? wsum[w - 1] : 0);
+      for (int i = b0; i < b1; ++i) {
+        const int c = start[i];
+        start[i] = run;
+        run += c;
+      }
+    }
+    __syncthreads();
+    // place: afterwards start[lc] is the END of slot lc (= old start[lc + 1])
+#pragma unroll
+    for (int u = 0; u < RPT; ++u) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int lc = sl[u][q];
+        if (lc < 0) continue;
+        const int pos = atomicAdd(&start[lc], 1);
+        P2 fy;
+        fy.x = rc[u].a;
+        fy.y = rc[u].b;
+        sfy[pos] = fy;
+        slc[pos] = (short)lc;
+      }
+    }
+    __syncthreads();
+    // gather: cell c_l (local) takes slots c_l .. c_l + 2m - 1
+#pragma unroll
+    for (int q = 0; q < kGridMaxCpt; ++q) {
+      const int cl = threadIdx.x + q * kGridThreads;
+      if (q >= cpt || cl >= TL) continue;
+      const int rb = cl == 0 ? 0 : start[cl - 1];
+      const int re = start[cl + 2 * m - 1];
+      T a = (T)0;
+      const int ctr = cl + m;
+#pragma unroll 2
+      for (int r = rb; r < re; ++r) {
+        const P2 fy = sfy[r];
+        const T dd = (T)(ctr - (int)slc[r]) - fy.x;
+        a += gauss_w(fy.y, dd, e.k1);
+      }
+      acc[q] += a;
+    }
+    __syncthreads();
   }
-  __syncthreads();
   T *out = grid + base;
-  for (int c = threadIdx.x; c < TL; c += blockDim.x) out[c] = acc[c];
+#pragma unroll
+  for (int q = 0; q < kGridMaxCpt; ++q)
+    if (q < cpt && threadIdx.x + q * kGridThreads < TL) out[threadIdx.x + q * kGridThreads] = acc[q];
+}
+
+template <typename T> size_t grid_smem_bytes(int logTL, int m) {
+  const int W = (1 << logTL) + 2 * m;
+  const size_t CAP = GridCfg<T>::CAP;
+  return sizeof(int) * ((W + 2 + 3) & ~3) + sizeof(T) * 2 * CAP + sizeof(short) * CAP;
 }
 
 // Last four-step pass of the packed real transform: CTA owns row pairs
 // (p, L1 - p), p in [p0, p0 + P), so both Z[k] and Z[L - k] are on chip.
+template <typename T> struct PairRowSrc {
+  const typename CxOf<T>::type *p;
+  int logL2, L1, p0, npairs;
+  __device__ __forceinline__ typename CxOf<T>::type load(int seq, int i) const {
+    const int pp = p0 + (seq >> 1);
+    const int row = (seq & 1) ? ((L1 - pp) & (L1 - 1)) : pp;
+    return pp < npairs ? p[((int64_t)row << logL2) + i] : cmk((T)0, (T)0);
+  }
+};
+
 template <typename T>
-__global__ void __launch_bounds__(512) k_fft_rowpass_acc(const typename CxOf<T>::type *__restrict__ in,
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_fft_rowpass_acc(const typename CxOf<T>::type *__restrict__ in,
                                                          FftDev<T> f, AccParams<T> e,
                                                          typename CxOf<T>::type *F) {
   typedef typename CxOf<T>::type C;
@@ -228,14 +377,8 @@ __global__ void __launch_bounds__(512) k_fft_rowpass_acc(const typename CxOf<T>:
   const int pitch = fft_pitch(L2, B);
   const int p0 = blockIdx.x * P, npairs = L1 / 2 + 1;
   const int tot = B << f.logL2;
-  for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
-    const int seq = idx >> f.logL2, n2 = idx & (L2 - 1);
-    const int p = p0 + (seq >> 1);
-    const int row = (seq & 1) ? ((L1 - p) & (L1 - 1)) : p;
-    s[seq * pitch + pad16(n2)] = p < npairs ? in[(int64_t)row * L2 + n2] : cmk((T)0, (T)0);
-  }
-  __syncthreads();
-  smem_fft<T>(s, pitch, f.logL2, B, f.tw2);
+  PairRowSrc<T> src{in, f.logL2, L1, p0, npairs};
+  fft_fused<T, false, false, false>(s, pitch, f.logL2, logB, f.tw2, src, NoDst());
   for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
     const int i = idx & (P - 1), half = (idx >> logP) & 1, k2 = idx >> (logP + 1);
     const int p = p0 + i;
@@ -414,8 +557,13 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     k_scan_tiles<<<1, 1024, 0, st>>>(counts, offsets, cursor, ntiles);
     CUNA_CK(cudaGetLastError());
   }
-  const size_t smg = sizeof(T) * ((size_t(1) << p->logTL) + 2 * p->m + 2);
-  k_grid_acc<T><<<ntiles, 256, smg, st>>>(recs, offsets, grid, e);
+  const size_t smg = grid_smem_bytes<T>(p->logTL, p->m);
+  static bool attr3 = false;
+  if (!attr3) {
+    CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr3 = true;
+  }
+  k_grid_acc<T><<<ntiles, kGridThreads, smg, st>>>(recs, offsets, grid, e);
   CUNA_CK(cudaGetLastError());
   mark(pr, "grid", st);
   // packed complex view of the real grid

@@ -17,9 +17,12 @@
 // bucket indices are bit-exact); only the order of records inside a tile
 // depends on scheduling.
 //
-// A Sampler provides `int64_t n` and
-//   __device__ void prep(int64_t i, Prep<Rec>& p)
-// filling p.nt (0..2), p.t[0..nt) and p.rec.
+// A Sampler provides `int64_t n`, a `Raw` struct of per-sample inputs and
+//   __device__ Raw  load(int64_t i, bool with_value)
+//   __device__ void prep(int64_t i, const Raw& r, Prep<Rec>& p)
+// prep fills p.nt (0..2), p.t[0..nt) and p.rec.  The kernels issue the loads
+// of all of a thread's samples before computing any of them, so that every
+// warp keeps several global loads in flight.
 #pragma once
 #include "common.cuh"
 
@@ -28,6 +31,7 @@ namespace {
 
 constexpr int kBinSmemTiles = 6144;  // shared histogram limit (scatter: 2 x 24 KB)
 constexpr int kScatterItems = 4;     // samples per thread in k_bin_scatter
+constexpr int kCountItems = 8;       // samples per thread in k_bin_count
 
 template <typename Rec> struct Prep {
   int nt;
@@ -43,13 +47,24 @@ __global__ void __launch_bounds__(512) k_bin_count(S smp, int *__restrict__ coun
     for (int t = threadIdx.x; t < ntiles; t += blockDim.x) lc[t] = 0;
     __syncthreads();
   }
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < smp.n; i += stride) {
-    Prep<typename S::Rec> p;
-    smp.prep(i, p);
-    for (int q = 0; q < p.nt; ++q) {
-      if (sm) atomicAdd(&lc[p.t[q]], 1);
-      else atomicAdd(&counts[p.t[q]], 1);
+  const int64_t span = (int64_t)blockDim.x * kCountItems;
+  for (int64_t c0 = (int64_t)blockIdx.x * span; c0 < smp.n; c0 += (int64_t)gridDim.x * span) {
+    typename S::Raw raw[kCountItems];
+#pragma unroll
+    for (int it = 0; it < kCountItems; ++it) {
+      const int64_t i = c0 + (int64_t)it * blockDim.x + threadIdx.x;
+      if (i < smp.n) raw[it] = smp.load(i, false);
+    }
+#pragma unroll
+    for (int it = 0; it < kCountItems; ++it) {
+      const int64_t i = c0 + (int64_t)it * blockDim.x + threadIdx.x;
+      if (i >= smp.n) continue;
+      Prep<typename S::Rec> p;
+      smp.prep(i, raw[it], p);
+      for (int q = 0; q < p.nt; ++q) {
+        if (sm) atomicAdd(&lc[p.t[q]], 1);
+        else atomicAdd(&counts[p.t[q]], 1);
+      }
     }
   }
   if (sm) {
@@ -114,11 +129,17 @@ __global__ void __launch_bounds__(512) k_bin_scatter(S smp, const int *__restric
   const int64_t chunk0 = (int64_t)blockIdx.x * blockDim.x * kScatterItems;
   Prep<Rec> p[kScatterItems];
   int rk[kScatterItems][2];
+  typename S::Raw raw[kScatterItems];
+#pragma unroll
+  for (int it = 0; it < kScatterItems; ++it) {
+    const int64_t i = chunk0 + (int64_t)it * blockDim.x + threadIdx.x;
+    if (i < smp.n) raw[it] = smp.load(i, true);
+  }
 #pragma unroll
   for (int it = 0; it < kScatterItems; ++it) {
     const int64_t i = chunk0 + (int64_t)it * blockDim.x + threadIdx.x;
     p[it].nt = 0;
-    if (i < smp.n) smp.prep(i, p[it]);
+    if (i < smp.n) smp.prep(i, raw[it], p[it]);
     for (int q = 0; q < p[it].nt; ++q) {
       const int t = p[it].t[q];
       rk[it][q] = sm ? atomicAdd(&lc[t], 1) : offsets[t] + atomicAdd(&cursor[t], 1);

@@ -127,15 +127,28 @@ template <typename T> __device__ __forceinline__ void set_val(RecD &r, double v)
 template <typename T, bool BOOT> struct SampCompat {
   typedef typename RecOf<T>::type Rec;
   typedef typename FpOf<T>::type FP;
+  struct Raw {
+    T x, y, E1, E2;
+  };
   const T *x;
   const T *y;
   const FP *fp;
   int64_t n;
   int ng;
-  __device__ __forceinline__ void prep(int64_t i, Prep<Rec> &p) const {
+  __device__ __forceinline__ Raw load(int64_t i, bool with_value) const {
+    Raw r;
+    r.x = x[i];
+    if (!BOOT && with_value) {
+      r.y = y ? y[i] : (T)1.0;
+      r.E1 = fp->E1[i];
+      r.E2 = fp->E2[i];
+    }
+    return r;
+  }
+  __device__ __forceinline__ void prep(int64_t i, const Raw &r, Prep<Rec> &p) const {
     int j, ms, me;
     p.nt = 0;
-    if (!compat_taps((double)x[i], ng, fp->filter_radius, !BOOT, j, ms, me)) return;
+    if (!compat_taps((double)r.x, ng, fp->filter_radius, !BOOT, j, ms, me)) return;
     const int t0 = (j + ms) >> kCompatLogTL, t1 = (j + me - 1) >> kCompatLogTL;
     p.t[0] = t0;
     p.t[1] = t1;
@@ -144,9 +157,9 @@ template <typename T, bool BOOT> struct SampCompat {
     if (BOOT) {
       p.rec.p = (int)i;
     } else {
-      p.rec.a = fp->E1[i];
-      p.rec.b = fp->E2[i];
-      set_val<T>(p.rec, y ? y[i] : (T)1.0);
+      p.rec.a = r.E1;
+      p.rec.b = r.E2;
+      set_val<T>(p.rec, r.y);
     }
   }
 };
@@ -219,6 +232,23 @@ __global__ void __launch_bounds__(256) k_grid_compat(const typename RecOf<T>::ty
 // ---------------------------------------------------------------------------
 // FFT with the reference deconvolution fused in
 // ---------------------------------------------------------------------------
+template <typename T> struct FacDst {
+  typename CxOf<T>::type *p;
+  int ng, logL1, r0, norm;
+  T b, nf;
+  __device__ __forceinline__ void store(int seq, int k2, typename CxOf<T>::type v) const {
+    const int k = r0 + seq + (k2 << logL1);
+    p[k] = norm ? cscale(v, compat_fac(k, ng, b, nf)) : v;
+  }
+};
+template <typename T> struct RowSrc {
+  const typename CxOf<T>::type *p;
+  int logL2;
+  __device__ __forceinline__ typename CxOf<T>::type load(int seq, int i) const {
+    return p[((int64_t)seq << logL2) + i];
+  }
+};
+
 template <typename T>
 __global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512) k_fft_single_compat(typename CxOf<T>::type *data, FftDev<T> f,
                                                             const typename FpOf<T>::type *fp, int norm) {
@@ -227,44 +257,28 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512) k_fft_single_comp
   C *s = reinterpret_cast<C *>(smem_raw);
   const int L = 1 << f.logL;
   C *d = data + (int64_t)blockIdx.x * L;
-  for (int i = threadIdx.x; i < L; i += blockDim.x) s[pad16(i)] = d[i];
-  __syncthreads();
-  smem_fft<T>(s, 0, f.logL, 1, f.tw1);
-  const T b = fp->b, nf = fp->normfac;
-  for (int k = threadIdx.x; k < L; k += blockDim.x)
-    d[k] = norm ? cscale(s[pad16(k)], compat_fac(k, L, b, nf)) : s[pad16(k)];
+  // in place: every read of d precedes the first barrier, every write follows it
+  RowSrc<T> src{d, 0};
+  FacDst<T> dst{d, L, 0, 0, norm, fp->b, fp->normfac};
+  fft_fused<T, true, false, false>(s, 0, f.logL, 0, f.tw1, src, dst);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(512) k_fft_rowpass_compat(const typename CxOf<T>::type *in,
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_fft_rowpass_compat(const typename CxOf<T>::type *in,
                                                             typename CxOf<T>::type *out, FftDev<T> f,
                                                             const typename FpOf<T>::type *fp,
                                                             int64_t slab_stride, int norm) {
   typedef typename CxOf<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *s = reinterpret_cast<C *>(smem_raw);
-  const int L2 = 1 << f.logL2;
   const int logB = ilog2i((int64_t)blockDim.x * kFftE) - f.logL2;
   const int B = 1 << logB;
-  const int pitch = fft_pitch(L2, B);
+  const int pitch = fft_pitch(1 << f.logL2, B);
   const int r0 = blockIdx.x * B;
-  const C *src = in + blockIdx.y * slab_stride + (int64_t)r0 * L2;
-  C *dst = out + blockIdx.y * slab_stride;
-  const int tot = B << f.logL2;
-  for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
-    const int row = idx >> f.logL2, n2 = idx & (L2 - 1);
-    s[row * pitch + pad16(n2)] = src[idx];
-  }
-  __syncthreads();
-  smem_fft<T>(s, pitch, f.logL2, B, f.tw2);
-  const T b = fp->b, nf = fp->normfac;
-  const int L = 1 << f.logL;
-  for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
-    const int k2 = idx >> logB, rl = idx & (B - 1);
-    const int k = r0 + rl + (k2 << f.logL1);
-    const C v = s[rl * pitch + pad16(k2)];
-    dst[k] = norm ? cscale(v, compat_fac(k, L, b, nf)) : v;
-  }
+  RowSrc<T> src{in + blockIdx.y * slab_stride + ((int64_t)r0 << f.logL2), f.logL2};
+  FacDst<T> dst{out + blockIdx.y * slab_stride, 1 << f.logL, f.logL1, r0, norm, fp->b, fp->normfac};
+  // rows are read point-fastest (contiguous), outputs written row-fastest
+  fft_fused<T, true, false, true>(s, pitch, f.logL2, logB, f.tw2, src, dst);
 }
 
 template <typename T>

@@ -172,6 +172,107 @@ __device__ void smem_fft(typename CxOf<T>::type *s, int pitch, int logL, int nse
     fft_stage<T, 16>(s, pitch, logL, logNs, total >> 4, tw);
 }
 
+// ---------------------------------------------------------------------------
+// Stockham FFT whose first stage reads its inputs straight from global memory
+// and whose last stage writes straight to global memory (through functors),
+// so a pass touches shared memory only between stages.
+//   Src: __device__ C load(int seq, int i)           input element i of seq
+//   Dst: __device__ void store(int seq, int k, C v)   output element k of seq
+// Each stage picks its own mapping of butterflies to threads: "seq fastest"
+// (consecutive threads take consecutive sequences, i.e. consecutive columns
+// of a row-major array) or "j fastest" (consecutive points of one sequence),
+// so that the global side of the first and last stage is coalesced.
+// ---------------------------------------------------------------------------
+template <typename T, int R, bool IN_G, bool OUT_G, bool SEQ_FAST, class Src, class Dst>
+__device__ __forceinline__ void fstage(typename CxOf<T>::type *s, int pitch, int logL, int logNs,
+                                       int logNseq, const typename CxOf<T>::type *__restrict__ tw,
+                                       const Src &src, const Dst &dst) {
+  typedef typename CxOf<T>::type C;
+  constexpr int LOGR = (R == 2) ? 1 : (R == 4) ? 2 : (R == 8) ? 3 : 4;
+  constexpr int NB = kFftE / R;
+  const int logLR = logL - LOGR;
+  const int total = 1 << (logNseq + logLR);
+  const int maskNs = (1 << logNs) - 1;
+  const int twsh = logL - logNs - LOGR;
+  C v[NB][R];
+#pragma unroll
+  for (int u = 0; u < NB; ++u) {
+    const int g = threadIdx.x + u * blockDim.x;
+    if (g < total) {
+      const int seq = SEQ_FAST ? (g & ((1 << logNseq) - 1)) : (g >> logLR);
+      const int j = SEQ_FAST ? (g >> logNseq) : (g & ((1 << logLR) - 1));
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int i = j + (r << logLR);
+        v[u][r] = IN_G ? src.load(seq, i) : s[seq * pitch + pad16(i)];
+      }
+      if (logNs > 0) {
+        const int k = j & maskNs;
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[u][r] = cmul(v[u][r], __ldg(&tw[(r * k) << twsh]));
+      }
+      dftR<R>(v[u]);
+    }
+  }
+  if (!IN_G && !OUT_G) __syncthreads();
+#pragma unroll
+  for (int u = 0; u < NB; ++u) {
+    const int g = threadIdx.x + u * blockDim.x;
+    if (g < total) {
+      const int seq = SEQ_FAST ? (g & ((1 << logNseq) - 1)) : (g >> logLR);
+      const int j = SEQ_FAST ? (g >> logNseq) : (g & ((1 << logLR) - 1));
+      const int idxD = ((j >> logNs) << (logNs + LOGR)) + (j & maskNs);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int k = idxD + (r << logNs);
+        if (OUT_G) dst.store(seq, k, v[u][r]);
+        else s[seq * pitch + pad16(k)] = v[u][r];
+      }
+    }
+  }
+  if (!OUT_G) __syncthreads();
+}
+
+template <typename T, int R, bool IN_G, bool OUT_G, bool FIRST_SEQ_FAST, bool LAST_SEQ_FAST, class Src, class Dst>
+__device__ __forceinline__ void fstage_sel(typename CxOf<T>::type *s, int pitch, int logL, int logNs,
+                                           int logNseq, const typename CxOf<T>::type *tw, const Src &src,
+                                           const Dst &dst) {
+  // first stages follow the load mapping, the last one the store mapping
+  if (OUT_G) fstage<T, R, IN_G, OUT_G, LAST_SEQ_FAST>(s, pitch, logL, logNs, logNseq, tw, src, dst);
+  else fstage<T, R, IN_G, OUT_G, FIRST_SEQ_FAST>(s, pitch, logL, logNs, logNseq, tw, src, dst);
+}
+
+// Full transform: Src -> [stages] -> Dst when TO_GLOBAL, or Src -> [stages] ->
+// shared memory (s[seq*pitch + pad16(k)], followed by a barrier) otherwise.
+template <typename T, bool TO_GLOBAL, bool FIRST_SEQ_FAST, bool LAST_SEQ_FAST, class Src, class Dst>
+__device__ void fft_fused(typename CxOf<T>::type *s, int pitch, int logL, int logNseq,
+                          const typename CxOf<T>::type *__restrict__ tw, const Src &src, const Dst &dst) {
+  int r0 = logL & 3;
+  if (r0 == 0) r0 = 4;
+  const bool single = r0 == logL;  // one stage only
+#define CUNA_FIRST(RR)                                                                          \
+  if (single) {                                                                                 \
+    fstage_sel<T, RR, true, TO_GLOBAL, FIRST_SEQ_FAST, LAST_SEQ_FAST>(s, pitch, logL, 0, logNseq, tw, src, dst); \
+    return;                                                                                     \
+  }                                                                                             \
+  fstage_sel<T, RR, true, false, FIRST_SEQ_FAST, LAST_SEQ_FAST>(s, pitch, logL, 0, logNseq, tw, src, dst);
+  switch (r0) {
+    case 1: { CUNA_FIRST(2) break; }
+    case 2: { CUNA_FIRST(4) break; }
+    case 3: { CUNA_FIRST(8) break; }
+    default: { CUNA_FIRST(16) break; }
+  }
+#undef CUNA_FIRST
+  int logNs = r0;
+  for (; logNs + 4 < logL; logNs += 4)
+    fstage_sel<T, 16, false, false, FIRST_SEQ_FAST, LAST_SEQ_FAST>(s, pitch, logL, logNs, logNseq, tw, src, dst);
+  fstage_sel<T, 16, false, TO_GLOBAL, FIRST_SEQ_FAST, LAST_SEQ_FAST>(s, pitch, logL, logNs, logNseq, tw, src, dst);
+}
+
+struct NoDst {
+  template <typename C> __device__ void store(int, int, C) const {}
+};
+
 // Device view of the twiddle tables of one transform length L = L1 * L2.
 template <typename T> struct FftDev {
   typedef typename CxOf<T>::type C;
@@ -191,36 +292,43 @@ __device__ __forceinline__ typename CxOf<T>::type twiddle_L(const FftDev<T> &f, 
 
 // ---------------------------------------------------------------------------
 // pass A: column FFTs of length L1 (stride L2), B = blockDim.x*E/L1 columns
-// per CTA, twiddle W_L^{n2 k1}, stored in place (in == out allowed).
+// per CTA, twiddle W_L^{n2 k1}, stored in place (in == out allowed: a CTA
+// reads all its columns before it writes any of them).
 // grid = (L2 / B, nslab)
 // ---------------------------------------------------------------------------
+template <typename T> struct ColSrc {
+  const typename CxOf<T>::type *p;
+  int L2, c0;
+  __device__ __forceinline__ typename CxOf<T>::type load(int seq, int i) const {
+    return p[(int64_t)i * L2 + c0 + seq];
+  }
+};
+template <typename T> struct ColDst {
+  typename CxOf<T>::type *p;
+  int L2, c0;
+  FftDev<T> f;
+  __device__ __forceinline__ void store(int seq, int k, typename CxOf<T>::type v) const {
+    p[(int64_t)k * L2 + c0 + seq] = cmul(v, twiddle_L(f, (c0 + seq) * k));
+  }
+};
+
 template <typename T>
-__global__ void __launch_bounds__(512) k_fft_colpass(const typename CxOf<T>::type *in,
-                                                     typename CxOf<T>::type *out, FftDev<T> f,
-                                                     int64_t slab_stride) {
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_fft_colpass(const typename CxOf<T>::type *in,
+                                                                            typename CxOf<T>::type *out,
+                                                                            FftDev<T> f, int64_t slab_stride) {
   typedef typename CxOf<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *s = reinterpret_cast<C *>(smem_raw);
-  const int L1 = 1 << f.logL1, L2 = 1 << f.logL2;
+  const int L2 = 1 << f.logL2;
   const int logB = ilog2i((int64_t)blockDim.x * kFftE) - f.logL1;
   const int B = 1 << logB;
-  const int pitch = fft_pitch(L1, B);
+  const int pitch = fft_pitch(1 << f.logL1, B);
   const int c0 = blockIdx.x * B;
-  const C *src = in + blockIdx.y * slab_stride;
-  C *dst = out + blockIdx.y * slab_stride;
-  const int tot = B << f.logL1;
-  for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
-    const int row = idx >> logB, col = idx & (B - 1);
-    s[col * pitch + pad16(row)] = src[(int64_t)row * L2 + c0 + col];
-  }
-  __syncthreads();
-  smem_fft<T>(s, pitch, f.logL1, B, f.tw1);
-  for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
-    const int k1 = idx >> logB, col = idx & (B - 1);
-    C v = s[col * pitch + pad16(k1)];
-    v = cmul(v, twiddle_L(f, (c0 + col) * k1));
-    dst[(int64_t)k1 * L2 + c0 + col] = v;
-  }
+  ColSrc<T> src{in + blockIdx.y * slab_stride, L2, c0};
+  ColDst<T> dst{out + blockIdx.y * slab_stride, L2, c0, f};
+  // a CTA's reads all precede the barrier after the first stage, its writes
+  // all follow it, so in == out is safe
+  fft_fused<T, true, true, true>(s, pitch, f.logL1, logB, f.tw1, src, dst);
 }
 
 }  // namespace
