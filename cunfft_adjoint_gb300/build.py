@@ -30,6 +30,7 @@ CORE_UNITS = [
     ("runtime.cu", []),
     ("compat.cu", ["--use_fast_math"]),
     ("accurate.cu", []),
+    ("batch.cu", []),
 ]
 
 LIBS = ["libcuna_gb300.so", "libcunaf.so", "libcunad.so"]

@@ -1,0 +1,526 @@
+// batch.cu -- batched accurate-mode adjoint NFFTs of many series of uneven
+// length (cuna2_batch_*).
+//
+// A batch plan fixes, per series s, its sample count n_s, its output count
+// nf_s (shared R and m), and its time origin/period (t0_s, T_s).  Samples of
+// all series are concatenated in t and y, outputs in F (offsets are prefix
+// sums).  One execution is a fixed set of work-list launches for the whole
+// batch, independent of the number of series:
+//
+//   series with ng_s <= 2^15 (float) / 2^14 (double): k_bsmall, one CTA per
+//     series (gridding in shared memory, FFT, epilogue), one launch per grid
+//     size class, on a forked stream so they overlap the large series;
+//   larger series: k_bcount / k_scan_tiles / k_bscatter (tile bucket sort over
+//     one global tile space), k_bgrid (a CTA per tile of any series),
+//     k_bcolpass / k_browpass (a CTA per column / row-pair block of any
+//     series) -- each CTA reads its series' parameters from a descriptor table.
+//
+// With cuna2_batch_set_graph the launch sequence is captured once per
+// argument set and replayed as one CUDA graph.
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <vector>
+#include "accurate_kernels.cuh"
+
+namespace cuna {
+namespace {
+
+template <typename T> struct BDesc {
+  AccParams<T> e;
+  PhaseMul pm;
+  FftDev<T> f;
+  int64_t s_off, n;  // samples [s_off, s_off + n) of t and y
+  int64_t g_off;     // first real grid cell of this series in the batch grid
+  int64_t f_off;     // first output of this series in F
+  int tile0, ntiles;  // global tile range of a large series
+};
+
+struct Item {
+  int s;     // series
+  int a, b;  // sample range [a, b) (binning) or block index a (FFT passes)
+  int pad;
+};
+
+constexpr int kBChunk = 2048;  // samples per binning CTA (512 threads x 4)
+
+template <typename T>
+__global__ void __launch_bounds__(512) k_bcount(const double *__restrict__ t, const T *__restrict__ y,
+                                                const BDesc<T> *__restrict__ D, const Item *__restrict__ items,
+                                                int *__restrict__ counts) {
+  extern __shared__ int lc[];
+  const Item it = items[blockIdx.x];
+  const BDesc<T> d = D[it.s];
+  for (int u = threadIdx.x; u < d.ntiles; u += blockDim.x) lc[u] = 0;
+  __syncthreads();
+  SampAcc<T> smp{t + d.s_off, y + d.s_off, d.n, d.pm, d.e};
+  typename SampAcc<T>::Raw raw[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int i = it.a + threadIdx.x + k * blockDim.x;
+    if (i < it.b) raw[k] = smp.load(i, false);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int i = it.a + threadIdx.x + k * blockDim.x;
+    if (i >= it.b) continue;
+    Prep<typename SampAcc<T>::Rec> p;
+    smp.prep(i, raw[k], p);
+    for (int q = 0; q < p.nt; ++q) atomicAdd(&lc[p.t[q]], 1);
+  }
+  __syncthreads();
+  for (int u = threadIdx.x; u < d.ntiles; u += blockDim.x)
+    if (lc[u]) atomicAdd(&counts[d.tile0 + u], lc[u]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) k_bscatter(const double *__restrict__ t, const T *__restrict__ y,
+                                                  const BDesc<T> *__restrict__ D, const Item *__restrict__ items,
+                                                  const int *__restrict__ offsets, int *__restrict__ cursor,
+                                                  typename RecOf<T>::type *__restrict__ recs) {
+  typedef typename RecOf<T>::type Rec;
+  extern __shared__ int sh[];
+  const Item it = items[blockIdx.x];
+  const BDesc<T> d = D[it.s];
+  int *lc = sh, *lbase = sh + d.ntiles;
+  for (int u = threadIdx.x; u < d.ntiles; u += blockDim.x) lc[u] = 0;
+  __syncthreads();
+  SampAcc<T> smp{t + d.s_off, y + d.s_off, d.n, d.pm, d.e};
+  typename SampAcc<T>::Raw raw[4];
+  Prep<Rec> p[4];
+  int rk[4][2];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int i = it.a + threadIdx.x + k * blockDim.x;
+    if (i < it.b) raw[k] = smp.load(i, true);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int i = it.a + threadIdx.x + k * blockDim.x;
+    p[k].nt = 0;
+    if (i < it.b) smp.prep(i, raw[k], p[k]);
+    for (int q = 0; q < p[k].nt; ++q) rk[k][q] = atomicAdd(&lc[p[k].t[q]], 1);
+  }
+  __syncthreads();
+  for (int u = threadIdx.x; u < d.ntiles; u += blockDim.x)
+    if (lc[u]) lbase[u] = offsets[d.tile0 + u] + atomicAdd(&cursor[d.tile0 + u], lc[u]);
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    for (int q = 0; q < p[k].nt; ++q) recs[lbase[p[k].t[q]] + rk[k][q]] = p[k].rec;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 4 : 2) k_bgrid(
+    const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
+    const BDesc<T> *__restrict__ D, const int *__restrict__ tile_series) {
+  const int gt = blockIdx.x;
+  const BDesc<T> d = D[tile_series[gt]];
+  grid_tile_body<T>(recs, off[gt], off[gt + 1], (gt - d.tile0) << d.e.logTL, grid + d.g_off, d.e, nullptr, 0, 0, 1,
+                    0);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_bcolpass(T *grid, const BDesc<T> *__restrict__ D,
+                                                                         const Item *__restrict__ items) {
+  typedef typename CxOf<T>::type C;
+  const Item it = items[blockIdx.x];
+  const BDesc<T> d = D[it.s];
+  C *z = reinterpret_cast<C *>(grid + d.g_off);
+  colpass_body<T>(z, z, d.f, it.a);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_browpass(const T *grid, const BDesc<T> *__restrict__ D,
+                                                                         const Item *__restrict__ items,
+                                                                         typename CxOf<T>::type *F) {
+  typedef typename CxOf<T>::type C;
+  const Item it = items[blockIdx.x];
+  const BDesc<T> d = D[it.s];
+  rowpass_acc_body<T>(reinterpret_cast<const C *>(grid + d.g_off), d.f, d.e, F + d.f_off, it.a);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512) k_bsmall(const double *__restrict__ t,
+                                                                        const T *__restrict__ y,
+                                                                        const BDesc<T> *__restrict__ D,
+                                                                        const int *__restrict__ list,
+                                                                        typename CxOf<T>::type *F) {
+  const BDesc<T> d = D[list[blockIdx.x]];
+  nfft_small_body<T>(t + d.s_off, y + d.s_off, d.n, d.pm, d.e, d.f, F + d.f_off);
+}
+
+template <typename T> AccParams<T> series_params(int64_t nf, int R, int m, double tau, int logTL) {
+  AccParams<T> e;
+  const int64_t ng = nf * R;
+  e.ng = ng;
+  e.nf = nf;
+  e.K = nf / 2;
+  e.m = m;
+  e.logTL = logTL;
+  e.ntiles = (int)(ng >> logTL);
+  e.k1 = (T)(1.0 / (4.0 * tau * log(2.0)));
+  e.k2 = (T)(1.0 / (2.0 * tau * log(2.0)));
+  e.e3c = (T)(-1.0 / (4.0 * tau));
+  e.c0 = (T)(0.5 / sqrt(4.0 * kPi * tau));
+  e.c1 = (T)(4.0 * kPi * kPi * tau / ((double)ng * (double)ng));
+  e.twk = (T)(2.0 / (double)ng);
+  return e;
+}
+
+template <typename T> FftDev<T> geom_dev(const FftGeom &g) {
+  typedef typename CxOf<T>::type C;
+  FftDev<T> f;
+  f.logL = g.logL;
+  f.logL1 = g.logL1;
+  f.logL2 = g.logL2;
+  f.tw1 = (const C *)g.tw1;
+  f.tw2 = (const C *)g.tw2;
+  f.twlo = (const C *)g.twlo;
+  f.twhi = (const C *)g.twhi;
+  return f;
+}
+
+template <typename V> int upload(const std::vector<V> &h, void **d) {
+  const size_t bytes = sizeof(V) * (h.empty() ? 1 : h.size());
+  cudaError_t e = cudaMalloc(d, bytes);
+  if (e != cudaSuccess) return fail(CUNA2_ERROR_ALLOC, "batch plan table of %zu bytes: %s", bytes, cudaGetErrorString(e));
+  if (!h.empty()) {
+    e = cudaMemcpy(*d, h.data(), sizeof(V) * h.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail_cuda(e, "cudaMemcpy(batch plan table)");
+  }
+  return CUNA2_SUCCESS;
+}
+
+}  // namespace
+}  // namespace cuna
+
+struct cuna2_batch_plan_st {
+  int dtype, R, m, nseries;
+  double tau;
+  int64_t n_total = 0, f_total = 0;
+  std::vector<int64_t> n, nf;
+  std::vector<double> t0, T;
+  // large series
+  int tiles_total = 0;
+  int64_t large_samples = 0, grid_total = 0;
+  int n_count_items = 0, n_col_items = 0, n_row_items = 0;
+  size_t smem_col = 0, smem_row = 0, smem_bin = 0;
+  int max_large_tiles = 0;
+  // small series by grid size class (log2 of the packed length)
+  std::vector<std::pair<int, int>> small_classes;  // (logL, count)
+  std::vector<int> small_class_off;
+  // device tables
+  void *d_desc = nullptr, *d_count_items = nullptr, *d_tile_series = nullptr, *d_col_items = nullptr,
+       *d_row_items = nullptr, *d_small_list = nullptr;
+  void *host_desc = nullptr;  // host copy (plain memory) for time updates
+  size_t desc_bytes = 0;
+  // workspace
+  void *ws = nullptr;
+  int *counts = nullptr, *offsets = nullptr, *cursor = nullptr;
+  void *recs = nullptr, *grid = nullptr;
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool use_graph = false;
+  cudaStream_t cap_stream = nullptr;
+  struct GraphEntry {
+    const void *t, *y, *F;
+    cudaGraphExec_t exec;
+  };
+  std::vector<GraphEntry> graphs;
+  std::mutex mu;
+};
+
+namespace cuna {
+namespace {
+
+template <typename T> int batch_build(cuna2_batch_plan_st *p) {
+  typedef typename CxOf<T>::type C;
+  typedef typename RecOf<T>::type Rec;
+  const bool dbl = sizeof(T) == 8;
+  const int single_log = dbl ? kSingleLogF64 : kSingleLogF32;
+  const int elems = dbl ? kPassElemsF64 : kPassElemsF32;
+  std::vector<BDesc<T>> desc(p->nseries);
+  std::vector<Item> count_items, col_items, row_items;
+  std::vector<int> tile_series;
+  std::map<int, std::vector<int>> small;  // logL -> series
+  int64_t s_off = 0, f_off = 0, g_off = 0;
+  int tile0 = 0;
+  for (int s = 0; s < p->nseries; ++s) {
+    const int64_t nf = p->nf[s], ng = nf * p->R, L = ng / 2;
+    const int logL = ilog2i(L);
+    const bool is_small = logL <= single_log;
+    const int logTL = ng <= 8192 ? ilog2i(ng) : 12;
+    BDesc<T> &d = desc[s];
+    d.e = series_params<T>(nf, p->R, p->m, p->tau, logTL);
+    d.pm = phase_setup(p->t0[s], p->T[s]);
+    FftGeom g;
+    CUNA_TRY(fft_geometry(dbl, logL, &g));
+    d.f = geom_dev<T>(g);
+    d.s_off = s_off;
+    d.n = p->n[s];
+    d.f_off = f_off;
+    d.g_off = -1;
+    d.tile0 = 0;
+    d.ntiles = 0;
+    if (is_small) {
+      small[logL].push_back(s);
+    } else {
+      d.g_off = g_off;
+      d.tile0 = tile0;
+      d.ntiles = (int)(ng >> logTL);
+      if (d.ntiles > kBinSmemTiles)
+        return fail(CUNA2_ERROR_UNSUPPORTED, "series %d: grid of %lld cells exceeds the batched tile limit", s,
+                    (long long)ng);
+      p->max_large_tiles = std::max(p->max_large_tiles, d.ntiles);
+      for (int u = 0; u < d.ntiles; ++u) tile_series.push_back(s);
+      for (int64_t a = 0; a < d.n; a += kBChunk) count_items.push_back({s, (int)a, (int)std::min<int64_t>(d.n, a + kBChunk), 0});
+      const int L1 = 1 << g.logL1, L2 = 1 << g.logL2;
+      const int BA = elems / L1, BB = elems / L2, PB = BB / 2, npairs = L1 / 2 + 1;
+      for (int cb = 0; cb < L2 / BA; ++cb) col_items.push_back({s, cb, 0, 0});
+      for (int pb = 0; pb < (npairs + PB - 1) / PB; ++pb) row_items.push_back({s, pb, 0, 0});
+      p->smem_col = std::max(p->smem_col, sizeof(C) * (size_t)BA * fft_pitch(L1, BA));
+      p->smem_row = std::max(p->smem_row, sizeof(C) * (size_t)BB * fft_pitch(L2, BB));
+      tile0 += d.ntiles;
+      g_off += ng;
+      p->large_samples += d.n;
+    }
+    s_off += p->n[s];
+    f_off += nf;
+  }
+  p->n_total = s_off;
+  p->f_total = f_off;
+  p->tiles_total = tile0;
+  p->grid_total = g_off;
+  p->n_count_items = (int)count_items.size();
+  p->n_col_items = (int)col_items.size();
+  p->n_row_items = (int)row_items.size();
+  p->smem_bin = sizeof(int) * 2 * (size_t)std::max(1, p->max_large_tiles);
+  std::vector<int> small_list;
+  for (auto &kv : small) {
+    p->small_classes.push_back({kv.first, (int)kv.second.size()});
+    p->small_class_off.push_back((int)small_list.size());
+    small_list.insert(small_list.end(), kv.second.begin(), kv.second.end());
+  }
+  p->desc_bytes = sizeof(BDesc<T>) * desc.size();
+  p->host_desc = malloc(p->desc_bytes ? p->desc_bytes : 1);
+  if (!p->host_desc) return fail(CUNA2_ERROR_ALLOC, "host descriptor table");
+  memcpy(p->host_desc, desc.data(), p->desc_bytes);
+  CUNA_TRY(upload(desc, &p->d_desc));
+  CUNA_TRY(upload(count_items, &p->d_count_items));
+  CUNA_TRY(upload(tile_series, &p->d_tile_series));
+  CUNA_TRY(upload(col_items, &p->d_col_items));
+  CUNA_TRY(upload(row_items, &p->d_row_items));
+  CUNA_TRY(upload(small_list, &p->d_small_list));
+  // workspace: counts | offsets | cursor | records | grid
+  const size_t nt = (size_t)std::max(1, p->tiles_total);
+  const size_t o_off = align_up(sizeof(int) * nt), o_cur = o_off + align_up(sizeof(int) * (nt + 1));
+  const size_t o_rec = o_cur + align_up(sizeof(int) * nt);
+  const size_t o_grid = o_rec + align_up(sizeof(Rec) * 2 * (size_t)std::max<int64_t>(1, p->large_samples));
+  const size_t bytes = o_grid + sizeof(T) * (size_t)std::max<int64_t>(1, p->grid_total);
+  cudaError_t e = cudaMalloc(&p->ws, bytes);
+  if (e != cudaSuccess) return fail(CUNA2_ERROR_ALLOC, "batch workspace of %zu bytes: %s", bytes, cudaGetErrorString(e));
+  char *w = (char *)p->ws;
+  p->counts = (int *)w;
+  p->offsets = (int *)(w + o_off);
+  p->cursor = (int *)(w + o_cur);
+  p->recs = w + o_rec;
+  p->grid = w + o_grid;
+  CUNA_CK(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
+  CUNA_CK(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+  CUNA_CK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
+  return CUNA2_SUCCESS;
+}
+
+template <typename T>
+int batch_run(cuna2_batch_plan_st *p, const double *t, const T *y, typename CxOf<T>::type *F, cudaStream_t st) {
+  typedef typename CxOf<T>::type C;
+  typedef typename RecOf<T>::type Rec;
+  if ((p->n_total > 0 && (!t || !y)) || !F) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL array");
+  const BDesc<T> *D = (const BDesc<T> *)p->d_desc;
+  static bool attr = false;
+  if (!attr) {
+    CUNA_CK(cudaFuncSetAttribute(k_bsmall<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    CUNA_CK(cudaFuncSetAttribute(k_bgrid<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CUNA_CK(cudaFuncSetAttribute(k_bcolpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CUNA_CK(cudaFuncSetAttribute(k_browpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  // small series on the side stream, overlapping the large-series pipeline
+  if (!p->small_classes.empty()) {
+    CUNA_CK(cudaEventRecord(p->ev_fork, st));
+    CUNA_CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
+    for (size_t c = 0; c < p->small_classes.size(); ++c) {
+      const int logL = p->small_classes[c].first, cnt = p->small_classes[c].second;
+      const int L = 1 << logL;
+      const size_t smem = sizeof(C) * (size_t)fft_pitch(L, 1) + sizeof(T) * (2 * p->m + 2);
+      const int threads = std::max(32, std::min(1024, L / kFftE));
+      k_bsmall<T><<<cnt, threads, smem, p->side>>>(t, y, D, (const int *)p->d_small_list + p->small_class_off[c], F);
+      CUNA_CK(cudaGetLastError());
+    }
+    CUNA_CK(cudaEventRecord(p->ev_join, p->side));
+  }
+  if (p->tiles_total > 0) {
+    const int ntl = p->tiles_total;
+    CUNA_CK(cudaMemsetAsync(p->counts, 0, sizeof(int) * ntl, st));
+    if (p->n_count_items > 0) {
+      k_bcount<T><<<p->n_count_items, 512, p->smem_bin / 2, st>>>(t, y, D, (const Item *)p->d_count_items, p->counts);
+      CUNA_CK(cudaGetLastError());
+    }
+    k_scan_tiles<<<1, 1024, 0, st>>>(p->counts, p->offsets, p->cursor, ntl);
+    CUNA_CK(cudaGetLastError());
+    if (p->n_count_items > 0) {
+      k_bscatter<T><<<p->n_count_items, 512, p->smem_bin, st>>>(t, y, D, (const Item *)p->d_count_items, p->offsets,
+                                                               p->cursor, (Rec *)p->recs);
+      CUNA_CK(cudaGetLastError());
+    }
+    const size_t smg = grid_smem_bytes<T>(12, p->m);
+    k_bgrid<T><<<ntl, kGridThreads, smg, st>>>((const Rec *)p->recs, p->offsets, (T *)p->grid, D,
+                                               (const int *)p->d_tile_series);
+    CUNA_CK(cudaGetLastError());
+    const int threads = (sizeof(T) == 4 ? kPassElemsF32 : kPassElemsF64) / kFftE;
+    k_bcolpass<T><<<p->n_col_items, threads, p->smem_col, st>>>((T *)p->grid, D, (const Item *)p->d_col_items);
+    CUNA_CK(cudaGetLastError());
+    k_browpass<T><<<p->n_row_items, threads, p->smem_row, st>>>((const T *)p->grid, D, (const Item *)p->d_row_items, F);
+    CUNA_CK(cudaGetLastError());
+  }
+  if (!p->small_classes.empty()) CUNA_CK(cudaStreamWaitEvent(st, p->ev_join, 0));
+  return CUNA2_SUCCESS;
+}
+
+int batch_any(cuna2_batch_plan_st *p, const double *t, const void *y, void *F, cudaStream_t st) {
+  if (p->dtype == CUNA2_F32) return batch_run<float>(p, t, (const float *)y, (float2 *)F, st);
+  return batch_run<double>(p, t, (const double *)y, (double2 *)F, st);
+}
+
+int batch_graph(cuna2_batch_plan_st *p, const double *t, const void *y, void *F, cudaStream_t st) {
+  for (auto &g : p->graphs)
+    if (g.t == t && g.y == y && g.F == F) {
+      CUNA_CK(cudaGraphLaunch(g.exec, st));
+      return CUNA2_SUCCESS;
+    }
+  CUNA_TRY(batch_any(p, t, y, F, st));
+  if (!p->cap_stream) CUNA_CK(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking));
+  CUNA_CK(cudaStreamSynchronize(st));
+  CUNA_CK(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
+  int s = batch_any(p, t, y, F, p->cap_stream);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(p->cap_stream, &graph);
+  if (s) return s;
+  if (e != cudaSuccess) return fail_cuda(e, "cudaStreamEndCapture");
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail_cuda(e, "cudaGraphInstantiate");
+  if (p->graphs.size() >= 16) {
+    cudaGraphExecDestroy(p->graphs.front().exec);
+    p->graphs.erase(p->graphs.begin());
+  }
+  p->graphs.push_back({t, y, F, exec});
+  return CUNA2_SUCCESS;
+}
+
+void batch_free(cuna2_batch_plan_st *p) {
+  for (auto &g : p->graphs) cudaGraphExecDestroy(g.exec);
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+  if (p->side) cudaStreamDestroy(p->side);
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  if (p->ev_join) cudaEventDestroy(p->ev_join);
+  for (void *d : {p->d_desc, p->d_count_items, p->d_tile_series, p->d_col_items, p->d_row_items, p->d_small_list,
+                  p->ws})
+    if (d) cudaFree(d);
+  free(p->host_desc);
+  delete p;
+}
+
+template <typename T> void set_times_host(cuna2_batch_plan_st *p) {
+  BDesc<T> *d = (BDesc<T> *)p->host_desc;
+  for (int s = 0; s < p->nseries; ++s) d[s].pm = phase_setup(p->t0[s], p->T[s]);
+}
+
+}  // namespace
+}  // namespace cuna
+
+using namespace cuna;
+
+extern "C" int cuna2_batch_plan_create(cuna2_batch_plan *plan, int dtype, int nseries, const int64_t *n,
+                                       const int64_t *nf, int R, int m, const double *t0, const double *T) {
+  clear_error();
+  if (!plan) return fail(CUNA2_ERROR_INVALID_VALUE, "plan pointer is NULL");
+  *plan = nullptr;
+  if (dtype != CUNA2_F32 && dtype != CUNA2_F64) return fail(CUNA2_ERROR_INVALID_VALUE, "dtype %d", dtype);
+  if (nseries < 1 || !n || !nf || R < 2 || m < 1 || m > 16)
+    return fail(CUNA2_ERROR_INVALID_VALUE, "need nseries >= 1, n and nf arrays, R >= 2, 1 <= m <= 16");
+  const int max_log = dtype == CUNA2_F32 ? 25 : 23;
+  for (int s = 0; s < nseries; ++s) {
+    const int64_t ng = nf[s] * R, L = ng / 2;
+    if (n[s] < 0 || n[s] > ((int64_t)1 << 30) || nf[s] < 2 || (nf[s] & 1) || (L & (L - 1)) || ng < 4 * m ||
+        ilog2i(L) > max_log)
+      return fail(CUNA2_ERROR_INVALID_VALUE, "series %d: unsupported n=%lld nf=%lld (R*nf/2 must be a power of two)",
+                  s, (long long)n[s], (long long)nf[s]);
+    if (T && !(T[s] > 0)) return fail(CUNA2_ERROR_INVALID_VALUE, "series %d: T must be > 0", s);
+  }
+  cuna2_batch_plan_st *p = new cuna2_batch_plan_st();
+  p->dtype = dtype;
+  p->R = R;
+  p->m = m;
+  p->nseries = nseries;
+  p->tau = (double)m * R / (4.0 * kPi * (R - 0.5));
+  p->n.assign(n, n + nseries);
+  p->nf.assign(nf, nf + nseries);
+  p->t0.assign(nseries, 0.0);
+  p->T.assign(nseries, 1.0);
+  if (t0) p->t0.assign(t0, t0 + nseries);
+  if (T) p->T.assign(T, T + nseries);
+  int st = dtype == CUNA2_F32 ? batch_build<float>(p) : batch_build<double>(p);
+  if (st) {
+    batch_free(p);
+    return st;
+  }
+  *plan = p;
+  return CUNA2_SUCCESS;
+}
+
+extern "C" int cuna2_batch_plan_destroy(cuna2_batch_plan p) {
+  clear_error();
+  if (p) batch_free(p);
+  return CUNA2_SUCCESS;
+}
+
+extern "C" int cuna2_batch_set_times(cuna2_batch_plan p, const double *t0, const double *T) {
+  clear_error();
+  if (!p || !t0 || !T) return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  for (int s = 0; s < p->nseries; ++s)
+    if (!(T[s] > 0)) return fail(CUNA2_ERROR_INVALID_VALUE, "series %d: T must be > 0", s);
+  p->t0.assign(t0, t0 + p->nseries);
+  p->T.assign(T, T + p->nseries);
+  if (p->dtype == CUNA2_F32) set_times_host<float>(p);
+  else set_times_host<double>(p);
+  CUNA_CK(cudaDeviceSynchronize());  // no execution may be reading the table
+  CUNA_CK(cudaMemcpy(p->d_desc, p->host_desc, p->desc_bytes, cudaMemcpyHostToDevice));
+  return CUNA2_SUCCESS;
+}
+
+extern "C" int cuna2_batch_info(cuna2_batch_plan p, int64_t *n_total, int64_t *nf_total) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  if (n_total) *n_total = p->n_total;
+  if (nf_total) *nf_total = p->f_total;
+  return CUNA2_SUCCESS;
+}
+
+extern "C" int cuna2_batch_set_graph(cuna2_batch_plan p, int enable) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  std::lock_guard<std::mutex> lk(p->mu);
+  p->use_graph = enable != 0;
+  return CUNA2_SUCCESS;
+}
+
+extern "C" int cuna2_batch_adjoint(cuna2_batch_plan p, const double *t, const void *y, void *F, cudaStream_t st) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  std::lock_guard<std::mutex> lk(p->mu);
+  return p->use_graph ? batch_graph(p, t, y, F, st) : batch_any(p, t, y, F, st);
+}

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include "binning.cuh"
 #include "fft.cuh"
+#include "rng.cuh"
 #include "runtime.h"
 
 namespace cuna {
@@ -82,22 +83,6 @@ __device__ __forceinline__ double compat_fac(int k, int ng, double b, double nor
 
 __device__ __forceinline__ float cpow(float a, int m) { return powf(a, m); }
 __device__ __forceinline__ double cpow(double a, int m) { return pow(a, m); }
-
-// wang_hash and rand_XORSHIFT, src/gridding.cu:67-82
-__device__ __forceinline__ unsigned wang_hash(unsigned s) {
-  s = (s ^ 61u) ^ (s >> 16);
-  s *= 9u;
-  s = s ^ (s >> 4);
-  s *= 0x27d4eb2du;
-  s = s ^ (s >> 15);
-  return s;
-}
-__device__ __forceinline__ unsigned xorshift32(unsigned s) {
-  s ^= (s << 13);
-  s ^= (s >> 17);
-  s ^= (s << 5);
-  return s;
-}
 
 // Reference cell j = (int)((x + 0.5) * (ng - 1)) (double arithmetic,
 // src/gridding.cu:43,93) and the tap bounds of :53-58.  Returns false when the

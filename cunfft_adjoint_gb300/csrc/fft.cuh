@@ -312,10 +312,10 @@ template <typename T> struct ColDst {
   }
 };
 
+// Column FFTs [c0, c0 + B) of one slab; B = blockDim.x * kFftE / L1.
 template <typename T>
-__global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_fft_colpass(const typename CxOf<T>::type *in,
-                                                                            typename CxOf<T>::type *out,
-                                                                            FftDev<T> f, int64_t slab_stride) {
+__device__ __forceinline__ void colpass_body(const typename CxOf<T>::type *in, typename CxOf<T>::type *out,
+                                             const FftDev<T> &f, int cblock) {
   typedef typename CxOf<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *s = reinterpret_cast<C *>(smem_raw);
@@ -323,12 +323,19 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_fft_colpass(cons
   const int logB = ilog2i((int64_t)blockDim.x * kFftE) - f.logL1;
   const int B = 1 << logB;
   const int pitch = fft_pitch(1 << f.logL1, B);
-  const int c0 = blockIdx.x * B;
-  ColSrc<T> src{in + blockIdx.y * slab_stride, L2, c0};
-  ColDst<T> dst{out + blockIdx.y * slab_stride, L2, c0, f};
+  const int c0 = cblock * B;
+  ColSrc<T> src{in, L2, c0};
+  ColDst<T> dst{out, L2, c0, f};
   // a CTA's reads all precede the barrier after the first stage, its writes
   // all follow it, so in == out is safe
   fft_fused<T, true, true, true>(s, pitch, f.logL1, logB, f.tw1, src, dst);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_fft_colpass(const typename CxOf<T>::type *in,
+                                                                            typename CxOf<T>::type *out,
+                                                                            FftDev<T> f, int64_t slab_stride) {
+  colpass_body<T>(in + blockIdx.y * slab_stride, out + blockIdx.y * slab_stride, f, blockIdx.x);
 }
 
 }  // namespace

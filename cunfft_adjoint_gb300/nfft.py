@@ -42,20 +42,24 @@ class AdjointNFFT:
     def __call__(self, t, y, t0=None, T=None, out=None, stream=None):
         return self.adjoint(t, y, t0, T, out, stream)
 
-    def adjoint(self, t, y, t0=None, T=None, out=None, stream=None):
+    def _check(self, t, y, t0, T):
         if t.dtype != torch.float64 or not t.is_cuda:
             raise TypeError("t must be a float64 CUDA tensor")
         if y.dtype != self.dtype or not y.is_cuda:
             raise TypeError("y must be a %s CUDA tensor" % self.dtype)
         t = t.contiguous()
         y = y.contiguous()
-        n = t.numel()
-        if y.numel() != n:
+        if y.numel() != t.numel():
             raise ValueError("t and y differ in length")
         if t0 is None or T is None:
-            lo, hi = float(t.min()), float(t.max())
+            lo, hi = (float(t.min()), float(t.max())) if t.numel() else (0.0, 1.0)
             t0 = lo if t0 is None else t0
             T = (hi - lo if hi > lo else 1.0) if T is None else T
+        return t, y, t0, T
+
+    def adjoint(self, t, y, t0=None, T=None, out=None, stream=None):
+        t, y, t0, T = self._check(t, y, t0, T)
+        n = t.numel()
         if out is None:
             out = torch.empty(self.nf, dtype=self.cdtype, device=t.device)
         s = (stream if stream is not None else torch.cuda.current_stream(t.device)).cuda_stream
@@ -63,6 +67,81 @@ class AdjointNFFT:
                                              float(t0), float(T), s or None))
         return out
 
+    def bootstrap(self, t, y, nbs, seed=0, t0=None, T=None, out=None, stream=None):
+        """nbs resamples with replacement of (t, y); returns (nbs, nf)."""
+        t, y, t0, T = self._check(t, y, t0, T)
+        if out is None:
+            out = torch.empty((nbs, self.nf), dtype=self.cdtype, device=t.device)
+        s = (stream if stream is not None else torch.cuda.current_stream(t.device)).cuda_stream
+        _lib.check(_lib.core().cuna2_adjoint_bootstrap(self._h, t.data_ptr(), y.data_ptr(), out.data_ptr(),
+                                                       t.numel(), int(nbs), seed & 0xFFFFFFFF,
+                                                       float(t0), float(T), s or None))
+        return out
+
     def frequencies(self):
         """Integer frequency index k of each output bin."""
         return torch.arange(-self.nf // 2, self.nf // 2, dtype=torch.int64)
+
+
+class BatchAdjointNFFT:
+    """Adjoint NFFTs of many series of uneven length in one execution.
+
+    Series s has ``n[s]`` samples and ``nf[s]`` outputs (``R * nf[s] / 2`` a
+    power of two); samples of all series are concatenated in ``t``/``y`` and
+    outputs in the returned flat tensor (``split`` gives per-series views).
+    ``t0``/``T`` (per series) define ``x = (t - t0)/T - 1/2``.
+    """
+
+    def __init__(self, n, nf, R=2, m=8, t0=None, T=None, dtype=torch.float32, device=None, graph=False):
+        import numpy as np
+        self.n = np.ascontiguousarray(n, dtype=np.int64)
+        self.nf = np.ascontiguousarray(nf, dtype=np.int64)
+        if self.n.shape != self.nf.shape or self.n.ndim != 1:
+            raise ValueError("n and nf must be 1-D and of equal length")
+        self.dtype = dtype
+        self.cdtype = torch.complex64 if dtype == torch.float32 else torch.complex128
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        ns = len(self.n)
+        t0a = None if t0 is None else np.ascontiguousarray(t0, dtype=np.float64)
+        Ta = None if T is None else np.ascontiguousarray(T, dtype=np.float64)
+        self._h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.core().cuna2_batch_plan_create(
+                ctypes.byref(self._h), _lib.F32 if dtype == torch.float32 else _lib.F64, ns,
+                self.n.ctypes.data, self.nf.ctypes.data, int(R), int(m),
+                None if t0a is None else t0a.ctypes.data, None if Ta is None else Ta.ctypes.data))
+        if graph:
+            _lib.check(_lib.core().cuna2_batch_set_graph(self._h, 1))
+        self.f_off = np.concatenate([[0], np.cumsum(self.nf)])
+        self.s_off = np.concatenate([[0], np.cumsum(self.n)])
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.core().cuna2_batch_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = ctypes.c_void_p()
+
+    def set_times(self, t0, T):
+        import numpy as np
+        t0a = np.ascontiguousarray(t0, dtype=np.float64)
+        Ta = np.ascontiguousarray(T, dtype=np.float64)
+        _lib.check(_lib.core().cuna2_batch_set_times(self._h, t0a.ctypes.data, Ta.ctypes.data))
+
+    def __call__(self, t, y, out=None, stream=None):
+        if t.dtype != torch.float64 or y.dtype != self.dtype or not (t.is_cuda and y.is_cuda):
+            raise TypeError("t must be float64 and y %s CUDA tensors" % self.dtype)
+        if t.numel() != int(self.s_off[-1]) or y.numel() != t.numel():
+            raise ValueError("t and y must hold sum(n) samples")
+        t = t.contiguous()
+        y = y.contiguous()
+        if out is None:
+            out = torch.empty(int(self.f_off[-1]), dtype=self.cdtype, device=t.device)
+        s = (stream if stream is not None else torch.cuda.current_stream(t.device)).cuda_stream
+        _lib.check(_lib.core().cuna2_batch_adjoint(self._h, t.data_ptr(), y.data_ptr(), out.data_ptr(), s or None))
+        return out
+
+    def split(self, F):
+        return [F[int(self.f_off[i]):int(self.f_off[i + 1])] for i in range(len(self.nf))]

@@ -170,6 +170,15 @@ int cuna2_plan_info(cuna2_plan plan, int64_t *ng, double *tau);
 int cuna2_adjoint(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
                   double t0, double T, cudaStream_t stream);
 
+/* Bootstrap: nbs resamples of (t, y) drawn with replacement, resample b
+ * taking samples d = xorshift32(wang_hash(seed + b*n + i)) % n, i < n (the
+ * reference's draw stream, src/gridding.cu:67-82,101), each transformed like
+ * cuna2_adjoint into F[b*nf .. (b+1)*nf).  The positions are binned once per
+ * call; each resample grids the original samples weighted by their draw
+ * multiplicity.  Requires nbs <= 65535 and nbs*n < 2^31. */
+int cuna2_adjoint_bootstrap(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
+                            int nbs, unsigned int seed, double t0, double T, cudaStream_t stream);
+
 /* Same transform with HOST arrays (pinned or pageable): copies t and y to
  * plan-owned device staging buffers, runs on `stream`, copies F back and
  * synchronises the stream before returning. */
@@ -189,6 +198,31 @@ int cuna2_plan_set_graph(cuna2_plan plan, int enable);
 int cuna2_plan_profile(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
                        double t0, double T, cudaStream_t stream, float *stage_ms,
                        const char **stage_names, int max_stages, int *nstages);
+
+/* ---------------------------------------------------------------------- */
+/* batched accurate mode: many series of uneven length                     */
+/* ---------------------------------------------------------------------- */
+typedef struct cuna2_batch_plan_st *cuna2_batch_plan;
+
+/* Plan for nseries series: series s has n[s] samples and nf[s] outputs
+ * (R*nf[s]/2 a power of two), all sharing R and m; t0/T (host arrays, may be
+ * NULL for 0 and 1) give x = (t - t0[s])/T[s] - 1/2.  The samples of all
+ * series are concatenated in t and y (series s at offset n[0]+..+n[s-1]) and
+ * so are the outputs in F.  Builds the work tables and allocates the whole
+ * workspace up front. */
+int cuna2_batch_plan_create(cuna2_batch_plan *plan, int dtype, int nseries, const int64_t *n,
+                            const int64_t *nf, int R, int m, const double *t0, const double *T);
+int cuna2_batch_plan_destroy(cuna2_batch_plan plan);
+/* Replace every series' t0/T (host arrays; synchronises the device). */
+int cuna2_batch_set_times(cuna2_batch_plan plan, const double *t0, const double *T);
+/* Total samples and total outputs of the batch. */
+int cuna2_batch_info(cuna2_batch_plan plan, int64_t *n_total, int64_t *nf_total);
+/* enable != 0: capture the batch's launch sequence into a CUDA graph per
+ * (t, y, F) and replay it. */
+int cuna2_batch_set_graph(cuna2_batch_plan plan, int enable);
+/* All transforms of the batch, stream-ordered. */
+int cuna2_batch_adjoint(cuna2_batch_plan plan, const double *t, const void *y, void *F,
+                        cudaStream_t stream);
 
 #ifdef __cplusplus
 }

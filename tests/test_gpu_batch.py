@@ -1,0 +1,83 @@
+"""GPU tests of the batched forms: bootstrap resampling in accurate mode
+(cuna2_adjoint_bootstrap) and uneven batches of series (cuna2_batch_*),
+against the FP64 direct NDFT of the oracle.  Bar: 1e-5 relative L2 (float)."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nfft(native_built):
+    from cunfft_adjoint_gb300 import nfft as N
+    return N
+
+
+@pytest.mark.parametrize("n,nf,R,m,nbs", [(3000, 4096, 2, 8, 4), (20000, 65536, 2, 8, 3), (5000, 16384, 2, 8, 2)])
+def test_bootstrap_resamples_vs_ndft(nfft, oracle_lib, n, nf, R, m, nbs):
+    """Resample b uses samples d = xorshift32(wang_hash(seed + b*n + i)) % n
+    (the reference's draw stream) at their own times."""
+    rng = np.random.default_rng(n)
+    t = rng.uniform(0, 100.0, n)
+    y = (np.sin(2 * np.pi * t / 2.1) + rng.normal(0, 0.3, n)).astype(np.float32)
+    seed = 1234
+    plan = nfft.AdjointNFFT(nf, R, m, torch.float32)
+    F = plan.bootstrap(torch.as_tensor(t, device="cuda"), torch.as_tensor(y, device="cuda"), nbs, seed, 0.0, 100.0)
+    torch.cuda.synchronize()
+    F = F.cpu().numpy().astype(np.complex128)
+    draws = oracle_lib.bootstrap_draws(seed, n, nbs).reshape(nbs, n)
+    k = np.arange(-nf // 2, nf // 2)
+    sel = k if nf <= 4096 else np.sort(rng.choice(k, 256, replace=False))
+    for b in range(nbs):
+        d = draws[b]
+        D = oracle_lib.ndft(t[d], y[d].astype(np.float64), 0.0, 100.0, sel)
+        assert rel_l2(F[b, sel + nf // 2], D) < 1e-5, b
+
+
+def _batch_case(rng, ns, nmin, nmax, nf_cap):
+    n = np.exp(rng.uniform(np.log(nmin), np.log(nmax), ns)).astype(np.int64)
+    nf = np.minimum(2 ** np.ceil(np.log2(4 * n)).astype(np.int64), nf_cap)
+    T = np.exp(rng.uniform(np.log(10), np.log(3000), ns))
+    ts, ys = [], []
+    for i in range(ns):
+        t = rng.uniform(0, T[i], n[i])
+        y = rng.normal(0, 1, n[i]) + 0.5 * np.sin(2 * np.pi * t / rng.uniform(0.5, 50))
+        ts.append(t)
+        ys.append(y.astype(np.float32))
+    return n, nf, T, ts, ys
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_uneven_batch_vs_ndft(nfft, oracle_lib, graph):
+    rng = np.random.default_rng(11)
+    n, nf, T, ts, ys = _batch_case(rng, 24, 60, 30000, 1 << 16)
+    plan = nfft.BatchAdjointNFFT(n, nf, 2, 8, np.zeros(len(n)), T, torch.float32, graph=graph)
+    td = torch.as_tensor(np.concatenate(ts), device="cuda")
+    yd = torch.as_tensor(np.concatenate(ys), device="cuda")
+    F = plan(td, yd)
+    F2 = plan(td, yd)
+    torch.cuda.synchronize()
+    Fs = [f.cpu().numpy().astype(np.complex128) for f in plan.split(F)]
+    assert torch.equal(F, F2) or rel_l2(F2.cpu().numpy(), F.cpu().numpy()) < 1e-6
+    assert any(R * f > 32768 for R, f in zip([2] * len(nf), nf)) and any(2 * f <= 32768 for f in nf)
+    for i in range(len(n)):
+        k = np.arange(-nf[i] // 2, nf[i] // 2)
+        sel = k if nf[i] <= 2048 else np.sort(rng.choice(k, 128, replace=False))
+        D = oracle_lib.ndft(ts[i], ys[i].astype(np.float64), 0.0, T[i], sel)
+        assert rel_l2(Fs[i][sel + nf[i] // 2], D) < 1e-5, (i, n[i], nf[i])
+
+
+def test_uneven_batch_matches_single_plans(nfft):
+    """The batched execution equals the per-series plans (same kernels)."""
+    rng = np.random.default_rng(12)
+    n, nf, T, ts, ys = _batch_case(rng, 6, 1000, 40000, 1 << 16)
+    plan = nfft.BatchAdjointNFFT(n, nf, 2, 8, np.zeros(len(n)), T, torch.float32)
+    F = plan(torch.as_tensor(np.concatenate(ts), device="cuda"), torch.as_tensor(np.concatenate(ys), device="cuda"))
+    for i, Fi in enumerate(plan.split(F)):
+        single = nfft.AdjointNFFT(int(nf[i]), 2, 8, torch.float32)
+        Si = single(torch.as_tensor(ts[i], device="cuda"), torch.as_tensor(ys[i], device="cuda"), 0.0, T[i])
+        torch.cuda.synchronize()
+        assert rel_l2(Fi.cpu().numpy(), Si.cpu().numpy()) < 1e-6, i
