@@ -155,6 +155,61 @@ def stage_bytes(n, ng, nf, rec_bytes=16, elem=4):
     }
 
 
+def batched_legs(dev, steps):
+    """Batched forms: bootstrap (N=5000, 1024 resamples, Nf=32768, R=2, m=8)
+    and an uneven batch (4096 series, N log-uniform in [100, 1e5], Nf =
+    nextpow2(4N) capped at 2^18, R=2, m=8), float32, CUDA-graph replay.
+    Returns NFFT/s for each (CUDA events, inputs resident)."""
+    import torch
+    from cunfft_adjoint_gb300.nfft import AdjointNFFT, BatchAdjointNFFT
+    out = {}
+    rng = np.random.default_rng(3)
+    # bootstrap
+    n, nbs, nf = 5000, 1024, 32768
+    t = rng.uniform(0, 100.0, n)
+    y = (np.sin(2 * np.pi * t / 2.1) + rng.normal(0, 0.3, n)).astype(np.float32)
+    plan = AdjointNFFT(nf, 2, 8, torch.float32, device=dev)
+    td, yd = torch.as_tensor(t, device=dev), torch.as_tensor(y, device=dev)
+    F = torch.empty((nbs, nf), dtype=torch.complex64, device=dev)
+    for i in range(3):
+        plan.bootstrap(td, yd, nbs, i, 0.0, 100.0, out=F)
+    torch.cuda.synchronize()
+    k = max(3, min(20, steps // 50))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(k):
+        plan.bootstrap(td, yd, nbs, i, 0.0, 100.0, out=F)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / k
+    out["bootstrap"] = {"workload": "N=5000, 1024 resamples, Nf=32768, R=2, m=8", "value": nbs * 1000.0 / ms,
+                        "unit": UNIT, "ms_per_call": ms, "calls": k}
+    del F, plan
+    # uneven batch
+    ns = 4096
+    nser = np.exp(rng.uniform(np.log(100), np.log(1e5), ns)).astype(np.int64)
+    nfs = np.minimum(2 ** np.ceil(np.log2(4 * nser)).astype(np.int64), 1 << 18)
+    Ts = np.exp(rng.uniform(np.log(10), np.log(3000), ns))
+    tt = np.concatenate([rng.uniform(0, Ts[i], nser[i]) for i in range(ns)])
+    yy = rng.normal(0, 1, int(nser.sum())).astype(np.float32)
+    bp = BatchAdjointNFFT(nser, nfs, 2, 8, np.zeros(ns), Ts, torch.float32, device=dev, graph=True)
+    tdd, ydd = torch.as_tensor(tt, device=dev), torch.as_tensor(yy, device=dev)
+    FF = torch.empty(int(nfs.sum()), dtype=torch.complex64, device=dev)
+    for i in range(3):
+        bp(tdd, ydd, out=FF)
+    torch.cuda.synchronize()
+    k = max(3, min(10, steps // 100))
+    e0.record()
+    for i in range(k):
+        bp(tdd, ydd, out=FF)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / k
+    out["uneven"] = {"workload": "4096 series, N log-U[100,1e5] (total %d), Nf=nextpow2(4N)<=2^18, R=2, m=8"
+                     % int(nser.sum()), "value": ns * 1000.0 / ms, "unit": UNIT, "ms_per_call": ms, "calls": k}
+    return out
+
+
 def cpu_baseline(wl, budget_s=20.0):
     """The reference pipeline on the host cores (oracle CPU program)."""
     from oracle import oracle
@@ -361,6 +416,8 @@ def main():
         f64 = {"value": 1000.0 / ms64, "unit": UNIT, "ms_per_step": ms64, "rel_err_vs_fp64_ndft": err64,
                "steps": k64}
 
+    batched = batched_legs(dev, args.steps) if rank == 0 else None
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl)
@@ -386,6 +443,7 @@ def main():
             "gpu_launches": kernels_per_step * args.steps,
             "clocks": clk.summary(),
             "f64": f64,
+            "batched": batched,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

@@ -39,6 +39,9 @@ struct cuna2_plan_st {
   std::mutex mu;
   void *ws = nullptr;
   size_t ws_bytes = 0;
+  // workspace of the backward pass (two packed complex grids)
+  void *bws = nullptr;
+  size_t bws_bytes = 0;
   // device staging for cuna2_adjoint_host
   void *stage = nullptr;
   size_t stage_bytes = 0;
@@ -272,6 +275,7 @@ extern "C" int cuna2_plan_destroy(cuna2_plan p) {
   for (auto &g : p->graphs) cudaGraphExecDestroy(g.exec);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   if (p->ws) cudaFree(p->ws);
+  if (p->bws) cudaFree(p->bws);
   if (p->stage) cudaFree(p->stage);
   delete p;
   return CUNA2_SUCCESS;
@@ -418,4 +422,83 @@ extern "C" int cuna2_adjoint_bootstrap(cuna2_plan p, const double *t, const void
   if (p->dtype == CUNA2_F32)
     return adjoint_run<float>(p, t, (const float *)y, (float2 *)F, n, t0, T, st, nullptr, nbs, seed);
   return adjoint_run<double>(p, t, (const double *)y, (double2 *)F, n, t0, T, st, nullptr, nbs, seed);
+}
+
+namespace cuna {
+namespace {
+template <typename T>
+int backward_run(cuna2_plan_st *p, const double *t, const T *y, const typename CxOf<T>::type *G, T *gy, double *gt,
+                 int64_t n, double t0, double T_, cudaStream_t st) {
+  typedef typename CxOf<T>::type C;
+  if (n < 0 || (n > 0 && (!t || (gt && !y))) || !G || !(T_ > 0) || !std::isfinite(T_) || !std::isfinite(t0))
+    return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument (n=%lld T=%g)", (long long)n, T_);
+  if (n == 0 || (!gy && !gt)) return CUNA2_SUCCESS;
+  const PhaseMul pm = phase_setup(t0, T_);
+  const AccParams<T> e = make_params<T>(p);
+  const FftDev<T> f = to_dev<T>(p->geom);
+  BwdSpec<T> sp;
+  sp.G = G;
+  sp.ng = p->ng;
+  sp.K = p->nf / 2;
+  sp.c0b = (T)(1.0 / sqrt(4.0 * kPi * p->tau));
+  sp.c1 = (T)(4.0 * kPi * kPi * p->tau / ((double)p->ng * (double)p->ng));
+  sp.twk = (T)(2.0 / (double)p->ng);
+  const double tscale = (double)p->ng / T_;
+  const int L = 1 << p->geom.logL;
+  if (p->small) {
+    static bool attr = false;
+    if (!attr) {
+      CUNA_CK(cudaFuncSetAttribute(k_bwd_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+      attr = true;
+    }
+    const size_t smem = sizeof(C) * (size_t)fft_pitch(L, 1);
+    const int threads = std::max(32, std::min(sizeof(T) == 4 ? 1024 : 512, L / kFftE));
+    k_bwd_small<T><<<1, std::max(threads, 32), smem, st>>>(t, y, n, pm, e, sp, f, gy, gt, tscale);
+    CUNA_CK(cudaGetLastError());
+    return CUNA2_SUCCESS;
+  }
+  const size_t need = 2 * sizeof(C) * (size_t)L;
+  if (p->bws_bytes < need) {
+    if (p->bws) {
+      CUNA_CK(cudaDeviceSynchronize());
+      CUNA_CK(cudaFree(p->bws));
+      p->bws = nullptr;
+      p->bws_bytes = 0;
+    }
+    cudaError_t er = cudaMalloc(&p->bws, need);
+    if (er != cudaSuccess) return fail(CUNA2_ERROR_ALLOC, "backward workspace: %s", cudaGetErrorString(er));
+    p->bws_bytes = need;
+  }
+  C *z = (C *)p->bws, *r = z + L;
+  const int elems = sizeof(T) == 4 ? kPassElemsF32 : kPassElemsF64;
+  const int threads = elems / kFftE;
+  const int L1 = 1 << p->geom.logL1, L2 = 1 << p->geom.logL2;
+  const int BA = elems / L1, BB = elems / L2;
+  const size_t smemA = sizeof(C) * (size_t)BA * fft_pitch(L1, BA);
+  const size_t smemB = sizeof(C) * (size_t)BB * fft_pitch(L2, BB);
+  static bool attr2 = false;
+  if (!attr2) {
+    CUNA_CK(cudaFuncSetAttribute(k_bwd_colpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CUNA_CK(cudaFuncSetAttribute(k_bwd_rowpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr2 = true;
+  }
+  k_bwd_colpass<T><<<L2 / BA, threads, smemA, st>>>(sp, z, f);
+  CUNA_CK(cudaGetLastError());
+  k_bwd_rowpass<T><<<L1 / BB, threads, smemB, st>>>(z, r, f);
+  CUNA_CK(cudaGetLastError());
+  k_bwd_interp<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(t, y, n, pm, e, (const T *)r, gy, gt, tscale);
+  CUNA_CK(cudaGetLastError());
+  return CUNA2_SUCCESS;
+}
+}  // namespace
+}  // namespace cuna
+
+extern "C" int cuna2_adjoint_backward(cuna2_plan p, const double *t, const void *y, const void *G, void *grad_y,
+                                      double *grad_t, int64_t n, double t0, double T, cudaStream_t st) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (p->dtype == CUNA2_F32)
+    return backward_run<float>(p, t, (const float *)y, (const float2 *)G, (float *)grad_y, grad_t, n, t0, T, st);
+  return backward_run<double>(p, t, (const double *)y, (const double2 *)G, (double *)grad_y, grad_t, n, t0, T, st);
 }

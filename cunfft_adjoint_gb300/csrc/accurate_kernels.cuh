@@ -443,6 +443,173 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_fft_rowpass_acc(
 }
 
 // ---------------------------------------------------------------------------
+// Backward (vector-Jacobian product) of the accurate transform.
+//
+// With g_k = dL/dRe F_k + i dL/dIm F_k for the stored outputs,
+//   h_k = g_k (-1)^k / psi_hat(k),      R_c = Re sum_k h_k exp(-2 pi i k c / ng),
+//   dL/dy_j = sum_d R_{b+d} psi(d - f),
+//   dL/dt_j = (ng / T) y_j sum_d R_{b+d} (d - f) / (2 tau) psi(d - f),
+// d = -m+1..m, b + f = s_j the grid position.  R is real: with the Hermitian
+// part H_k = (h_k + conj(h_{-k})) / 2 of h, R = DFT_-(H) is computed as one
+// complex DFT of length L = ng/2 of Zin[k] = E[k] + i O[k], E[k] = H_k +
+// H_{k+L}, O[k] = (H_k - H_{k+L}) exp(-2 pi i k / ng), whose output is
+// R[2n] + i R[2n+1].  DFT_- = conj(DFT_+(conj(.))); the conjugations are fused
+// into the load and store functors of the (inverse-sign) FFT passes.
+// ---------------------------------------------------------------------------
+template <typename T> struct BwdSpec {
+  const typename CxOf<T>::type *G;  // nf values, G[k + nf/2]
+  int64_t ng, K;                     // K = nf / 2
+  T c0b, c1;                         // 1/psi_hat(k) = c0b exp(c1 k^2)
+  T twk;                             // 2 / ng
+  // h_k for any integer k (taken mod ng), zero outside the output band
+  __device__ __forceinline__ typename CxOf<T>::type h(int64_t k) const {
+    k %= ng;
+    if (k < 0) k += ng;
+    if (k >= ng - K) k -= ng;  // to [-K, ng - K)
+    if (k >= K || k < -K) return cmk((T)0, (T)0);
+    const T kf = (T)k;
+    T sc = c0b * exp_t(c1 * kf * kf);
+    if (k & 1) sc = -sc;
+    return cscale(G[k + K], sc);
+  }
+  // conj(Zin[q]), q in [0, L)
+  __device__ __forceinline__ typename CxOf<T>::type zin_conj(int64_t q) const {
+    typedef typename CxOf<T>::type C;
+    const int64_t L = ng / 2;
+    const C hq = h(q), hmq = h(-q), hp = h(q + L), hmp = h(-q - L);
+    const T half = (T)0.5;
+    const C Hq = cscale(cadd(hq, cconj(hmq)), half);   // H_q
+    const C Hp = cscale(cadd(hp, cconj(hmp)), half);   // H_{q+L}
+    const C E = cadd(Hq, Hp);
+    T sn, cs;
+    sincospi_t((T)q * twk, &sn, &cs);
+    const C O = cmul(csub(Hq, Hp), cmk(cs, -sn));      // (H_q - H_{q+L}) e^{-2 pi i q / ng}
+    return cconj(cadd(E, cmuli(O)));
+  }
+};
+
+// interpolation of R at one sample: accumulates both gradient sums
+template <typename T, class Rget>
+__device__ __forceinline__ void bwd_sample(const Rget &R, int cell, T fr, int m, int ng, T k1, T inv2tau,
+                                           T &sy, T &st) {
+  sy = (T)0;
+  st = (T)0;
+  for (int d = -m + 1; d <= m; ++d) {
+    int c = cell + d;
+    if (c < 0) c += ng;
+    else if (c >= ng) c -= ng;
+    const T dd = (T)d - fr;
+    const T w = R(c) * exp2_t(-k1 * dd * dd);
+    sy += w;
+    st += w * dd * inv2tau;
+  }
+}
+
+// Single CTA: spectrum -> shared memory -> FFT -> interpolation at every sample.
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512) k_bwd_small(
+    const double *__restrict__ t, const T *__restrict__ y, int64_t n, PhaseMul pm, AccParams<T> e, BwdSpec<T> sp,
+    FftDev<T> f, T *__restrict__ gy, double *__restrict__ gt, double tscale) {
+  typedef typename CxOf<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int L = 1 << f.logL;
+  const int pitch = fft_pitch(L, 1);
+  C *s = reinterpret_cast<C *>(smem_raw);
+  const T *sr = reinterpret_cast<const T *>(smem_raw);
+  for (int q = threadIdx.x; q < L; q += blockDim.x) s[pad16(q)] = sp.zin_conj(q);
+  __syncthreads();
+  smem_fft<T>(s, pitch, f.logL, 1, f.tw1);
+  // output z[nn] = conj(FFT result): R[2nn] = Re, R[2nn+1] = -Im
+  auto R = [&](int c) -> T {
+    const T v = sr[real_slot(c)];
+    return (c & 1) ? -v : v;
+  };
+  const T inv2tau = (T)2.0 * e.e3c * (T)-1.0;  // 1 / (2 tau) = -2 e3c
+  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+    int cell;
+    T fr;
+    reduce_sample<T>(t[j], pm, e.ng, cell, fr);
+    T a, b;
+    bwd_sample<T>(R, cell, fr, e.m, (int)e.ng, e.k1, inv2tau, a, b);
+    if (gy) gy[j] = a;
+    if (gt) gt[j] = tscale * (double)y[j] * (double)b;
+  }
+}
+
+// four-step pass A of the backward: columns of conj(Zin) computed from G on the fly
+template <typename T> struct SpecColSrc {
+  BwdSpec<T> sp;
+  int L2, c0;
+  __device__ __forceinline__ typename CxOf<T>::type load(int seq, int i) const {
+    return sp.zin_conj((int64_t)i * L2 + c0 + seq);
+  }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_bwd_colpass(BwdSpec<T> sp, typename CxOf<T>::type *z,
+                                                                            FftDev<T> f) {
+  typedef typename CxOf<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *s = reinterpret_cast<C *>(smem_raw);
+  const int L2 = 1 << f.logL2;
+  const int logB = ilog2i((int64_t)blockDim.x * kFftE) - f.logL1;
+  const int B = 1 << logB;
+  const int pitch = fft_pitch(1 << f.logL1, B);
+  const int c0 = blockIdx.x * B;
+  SpecColSrc<T> src{sp, L2, c0};
+  ColDst<T> dst{z, L2, c0, f};
+  fft_fused<T, true, true, true>(s, pitch, f.logL1, logB, f.tw1, src, dst);
+}
+
+// pass B: rows -> real field R (conjugated outputs, interleaved re/im)
+template <typename T> struct ConjRealDst {
+  typename CxOf<T>::type *r;  // R viewed as L complex values
+  int logL1, r0;
+  __device__ __forceinline__ void store(int seq, int k2, typename CxOf<T>::type v) const {
+    r[r0 + seq + (k2 << logL1)] = cconj(v);
+  }
+};
+template <typename T> struct PlainRowSrc {
+  const typename CxOf<T>::type *p;
+  int logL2;
+  __device__ __forceinline__ typename CxOf<T>::type load(int seq, int i) const {
+    return p[((int64_t)seq << logL2) + i];
+  }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_bwd_rowpass(const typename CxOf<T>::type *z,
+                                                                            typename CxOf<T>::type *r, FftDev<T> f) {
+  typedef typename CxOf<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *s = reinterpret_cast<C *>(smem_raw);
+  const int logB = ilog2i((int64_t)blockDim.x * kFftE) - f.logL2;
+  const int B = 1 << logB;
+  const int pitch = fft_pitch(1 << f.logL2, B);
+  const int r0 = blockIdx.x * B;
+  PlainRowSrc<T> src{z + ((int64_t)r0 << f.logL2), f.logL2};
+  ConjRealDst<T> dst{r, f.logL1, r0};
+  fft_fused<T, true, false, true>(s, pitch, f.logL2, logB, f.tw2, src, dst);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_bwd_interp(const double *__restrict__ t, const T *__restrict__ y, int64_t n,
+                                                    PhaseMul pm, AccParams<T> e, const T *__restrict__ R,
+                                                    T *__restrict__ gy, double *__restrict__ gt, double tscale) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  int cell;
+  T fr;
+  reduce_sample<T>(t[j], pm, e.ng, cell, fr);
+  const T inv2tau = (T)2.0 * e.e3c * (T)-1.0;
+  auto Rg = [&](int c) -> T { return __ldg(&R[c]); };
+  T a, b;
+  bwd_sample<T>(Rg, cell, fr, e.m, (int)e.ng, e.k1, inv2tau, a, b);
+  if (gy) gy[j] = a;
+  if (gt) gt[j] = tscale * (double)y[j] * (double)b;
+}
+
+// ---------------------------------------------------------------------------
 // bootstrap: resample b draws n indices d = xorshift32(wang_hash(seed + b*n +
 // i)) % n with replacement; gridding resample b is gridding every original
 // sample p with weight (number of times p was drawn) * y[p].

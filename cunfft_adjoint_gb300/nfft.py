@@ -78,6 +78,19 @@ class AdjointNFFT:
                                                        float(t0), float(T), s or None))
         return out
 
+    def backward(self, t, y, grad_F, t0, T, need_y=True, need_t=True, stream=None):
+        """(dL/dy, dL/dt) for grad_F = dL/dRe F + i dL/dIm F (torch's convention)."""
+        gy = torch.empty_like(y) if need_y else None
+        gt = torch.empty_like(t) if need_t else None
+        s = (stream if stream is not None else torch.cuda.current_stream(t.device)).cuda_stream
+        g = grad_F.contiguous()
+        if g.dtype != self.cdtype:
+            g = g.to(self.cdtype)
+        _lib.check(_lib.core().cuna2_adjoint_backward(
+            self._h, t.data_ptr(), y.data_ptr(), g.data_ptr(), None if gy is None else gy.data_ptr(),
+            None if gt is None else gt.data_ptr(), t.numel(), float(t0), float(T), s or None))
+        return gy, gt
+
     def frequencies(self):
         """Integer frequency index k of each output bin."""
         return torch.arange(-self.nf // 2, self.nf // 2, dtype=torch.int64)

@@ -179,6 +179,17 @@ int cuna2_adjoint(cuna2_plan plan, const double *t, const void *y, void *F, int6
 int cuna2_adjoint_bootstrap(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
                             int nbs, unsigned int seed, double t0, double T, cudaStream_t stream);
 
+/* Vector-Jacobian product of cuna2_adjoint for a real loss L(F): given
+ * G[k + nf/2] = dL/dRe F_k + i dL/dIm F_k (nf complex values of the plan's
+ * precision), writes dL/dy_j (n values of the plan's precision) to grad_y and
+ * dL/dt_j (n doubles) to grad_t; either may be NULL.  Uses the same Gaussian
+ * kernel: one FFT of the deconvolved spectrum to a real field on the grid,
+ * then per sample the kernel and its derivative interpolate it.  Nothing of
+ * the forward pass is stored or needed besides t and y. */
+int cuna2_adjoint_backward(cuna2_plan plan, const double *t, const void *y, const void *G,
+                           void *grad_y, double *grad_t, int64_t n, double t0, double T,
+                           cudaStream_t stream);
+
 /* Same transform with HOST arrays (pinned or pageable): copies t and y to
  * plan-owned device staging buffers, runs on `stream`, copies F back and
  * synchronises the stream before returning. */

@@ -479,3 +479,32 @@ void cuna_oracle_cpu_twiddles_f32(int64_t n, float *tw) {
     tw[2 * k + 1] = (float)sin(ang);
   }
 }
+
+/* ------------------------------------------------------------------------ */
+/* 6. FP64 direct-sum gradient of a real loss through the adjoint NDFT       */
+/* ------------------------------------------------------------------------ */
+
+/* For F_q = sum_j y_j exp(+2 pi i k_q x_j), x_j = (t_j - t0)/T - 1/2, and a
+ * real loss with g_q = dL/dRe F_q + i dL/dIm F_q (interleaved re/im):
+ *   dL/dy_j = Re sum_q conj(g_q) exp(2 pi i k_q x_j)
+ *   dL/dt_j = Re sum_q conj(g_q) y_j (2 pi i k_q / T) exp(2 pi i k_q x_j)  */
+void cuna_oracle_ndft_grad(const double *t, const double *y, int64_t n, double t0, double T,
+                           const int64_t *k, const double *g, int64_t nk, double *gy, double *gt) {
+#pragma omp parallel for schedule(static)
+  for (int64_t j = 0; j < n; ++j) {
+    const double x = (t[j] - t0) / T - 0.5;
+    double sy = 0.0, st = 0.0;
+    for (int64_t q = 0; q < nk; ++q) {
+      double ph = (double)k[q] * x;
+      ph -= nearbyint(ph);
+      const double c = cos(2.0 * M_PI * ph), s = sin(2.0 * M_PI * ph);
+      const double gr = g[2 * q], gi = g[2 * q + 1];
+      /* conj(g) e^{i phi} = (gr c + gi s) + i (gr s - gi c) */
+      const double re = gr * c + gi * s, im = gr * s - gi * c;
+      sy += re;
+      st += -im * (double)k[q]; /* Re(i k (re + i im)) = -k im */
+    }
+    gy[j] = sy;
+    gt[j] = y[j] * 2.0 * M_PI / T * st;
+  }
+}

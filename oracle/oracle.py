@@ -66,6 +66,7 @@ def _declare(L):
     L.cuna_oracle_accurate_tau.argtypes = [_I, _D]; L.cuna_oracle_accurate_tau.restype = _D
     L.cuna_oracle_accurate_adjoint.argtypes = [_P, _P, _I64, _D, _D, _I64, _I, _I, _P]
     L.cuna_oracle_ndft.argtypes = [_P, _P, _P, _I64, _D, _D, _P, _I64, _P]
+    L.cuna_oracle_ndft_grad.argtypes = [_P, _P, _I64, _D, _D, _P, _P, _I64, _P, _P]
     L.cuna_oracle_num_threads.restype = _I
     L.cuna_oracle_cpu_pipeline_f32.argtypes = [_P, _P, _I, _I, _P, _P, _P, _P, _P]
     L.cuna_oracle_cpu_twiddles_f32.argtypes = [_I64, _P]
@@ -198,6 +199,19 @@ def ndft(t, y, t0, T, k):
     lib().cuna_oracle_ndft(_p(t), _p(yr), _p(yi), len(t), float(t0), float(T), _p(k), len(k),
                            _p(F.view(np.float64)))
     return F
+
+
+def ndft_grad(t, y, t0, T, k, g):
+    """FP64 gradient (dL/dy, dL/dt) of a real loss through the direct adjoint
+    NDFT, given g_q = dL/dRe F_q + i dL/dIm F_q on frequencies k_q."""
+    t = np.ascontiguousarray(t, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    k = np.ascontiguousarray(k, np.int64)
+    g = np.ascontiguousarray(g, np.complex128)
+    gy = np.empty(len(t)); gt = np.empty(len(t))
+    lib().cuna_oracle_ndft_grad(_p(t), _p(y), len(t), float(t0), float(T), _p(k), _p(g.view(np.float64)),
+                                len(k), _p(gy), _p(gt))
+    return gy, gt
 
 
 def num_threads():
