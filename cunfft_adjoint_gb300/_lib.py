@@ -67,6 +67,8 @@ CORE_SIGNATURES = {
     "cuna2_adjoint_host": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P]),
     "cuna2_adjoint_bootstrap": (_I, [_P, _P, _P, _P, _I64, _I, _U, _D, _D, _P]),
     "cuna2_adjoint_backward": (_I, [_P, _P, _P, _P, _P, _P, _I64, _D, _D, _P]),
+    "cuna2_adjoint_multi": (_I, [_P, _P, _P, _P, _I64, _I, _D, _D, _P]),
+    "cuna2_lomb_scargle": (_I, [_I, _P, _P, _P, _I64, _I64, _D, _D, _I, _I, _P, _P]),
     "cuna2_plan_set_graph": (_I, [_P, _I]),
     "cuna2_plan_profile": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P, _P, _P, _I, _P]),
     "cuna2_batch_plan_create": (_I, [_P, _I, _I, _P, _P, _I, _I, _P, _P]),

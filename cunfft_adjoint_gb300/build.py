@@ -31,6 +31,7 @@ CORE_UNITS = [
     ("compat.cu", ["--use_fast_math"]),
     ("accurate.cu", []),
     ("batch.cu", []),
+    ("lombscargle.cu", []),
 ]
 
 LIBS = ["libcuna_gb300.so", "libcunaf.so", "libcunad.so"]

@@ -116,9 +116,13 @@ inline void mark(Prof *pr, const char *name, cudaStream_t st) {
 // One plan execution.  nbs == 0: a single transform of (t, y).  nbs >= 1:
 // bootstrap, nbs resamples with replacement of (t, y) from the seeded draw
 // stream, outputs F[b*nf + k].
+// With `multi` (nmulti channels of n values, channel-major), the channels are
+// transformed together: one binning pass, one gridding launch with a slab per
+// channel, one slab-batched FFT; outputs F[c*nf + k].
 template <typename T>
 int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>::type *F, int64_t n,
-                double t0, double T_, cudaStream_t st, Prof *pr = nullptr, int nbs = 0, unsigned seed = 0) {
+                double t0, double T_, cudaStream_t st, Prof *pr = nullptr, int nbs = 0, unsigned seed = 0,
+                const T *multi = nullptr, int nmulti = 0) {
   typedef typename CxOf<T>::type C;
   typedef typename RecOf<T>::type Rec;
   if (n < 0 || (n > 0 && (!t || !y)) || !F || !(T_ > 0) || !std::isfinite(T_) || !std::isfinite(t0))
@@ -127,7 +131,9 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   if (nbs < 0 || nbs > 65535 || (int64_t)nbs * n >= ((int64_t)1 << 31))
     return fail(CUNA2_ERROR_UNSUPPORTED, "bootstrap needs 1 <= nbs <= 65535 and nbs*n < 2^31");
   if (nbs > 0 && n == 0) return fail(CUNA2_ERROR_INVALID_VALUE, "bootstrap of an empty series");
-  const int nslab = nbs > 0 ? nbs : 1;
+  if (multi && (nmulti < 1 || nmulti > 65535 || nbs > 0))
+    return fail(CUNA2_ERROR_INVALID_VALUE, "multi-channel transform needs 1 <= nchan <= 65535");
+  const int nslab = multi ? nmulti : (nbs > 0 ? nbs : 1);
   const PhaseMul pm = phase_setup(t0, T_);
   const AccParams<T> e = make_params<T>(p);
   const FftDev<T> f = to_dev<T>(p->geom);
@@ -145,9 +151,9 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   int *counts = (int *)(w + o_cnt), *offsets = (int *)(w + o_off), *cursor = (int *)(w + o_cur);
   Rec *recs = (Rec *)(w + o_rec);
   T *grid = (T *)(w + o_grid);
-  T *wts = nbs > 0 ? (T *)(w + o_wts) : nullptr;
+  T *wts = multi ? const_cast<T *>(multi) : (nbs > 0 ? (T *)(w + o_wts) : nullptr);
   mark(pr, "start", st);
-  if (wts) {
+  if (nbs > 0) {
     static bool attrw = false;
     if (!attrw) {
       CUNA_CK(cudaFuncSetAttribute(k_boot_weights<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -199,8 +205,8 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr3 = true;
   }
-  // bootstrap: each CTA grids a group of resamples of one tile, reusing its sort
-  const int group = nbs > 0 ? std::min(8, nslab) : 1;
+  // bootstrap / channels: each CTA grids a group of slabs of one tile, reusing its sort
+  const int group = wts ? std::min(8, nslab) : 1;
   k_grid_acc<T><<<dim3(ntiles, (nslab + group - 1) / group), kGridThreads, smg, st>>>(
       recs, offsets, grid, e, wts, n, nslab, group, p->ng);
   CUNA_CK(cudaGetLastError());
@@ -501,4 +507,17 @@ extern "C" int cuna2_adjoint_backward(cuna2_plan p, const double *t, const void 
   if (p->dtype == CUNA2_F32)
     return backward_run<float>(p, t, (const float *)y, (const float2 *)G, (float *)grad_y, grad_t, n, t0, T, st);
   return backward_run<double>(p, t, (const double *)y, (const double2 *)G, (double *)grad_y, grad_t, n, t0, T, st);
+}
+
+extern "C" int cuna2_adjoint_multi(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, int nchan,
+                                   double t0, double T, cudaStream_t st) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  if (!y || nchan < 1) return fail(CUNA2_ERROR_INVALID_VALUE, "need nchan >= 1 value channels");
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (p->dtype == CUNA2_F32)
+    return adjoint_run<float>(p, t, (const float *)y, (float2 *)F, n, t0, T, st, nullptr, 0, 0, (const float *)y,
+                              nchan);
+  return adjoint_run<double>(p, t, (const double *)y, (double2 *)F, n, t0, T, st, nullptr, 0, 0,
+                             (const double *)y, nchan);
 }

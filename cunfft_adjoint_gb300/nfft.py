@@ -78,6 +78,20 @@ class AdjointNFFT:
                                                        float(t0), float(T), s or None))
         return out
 
+    def multi(self, t, Y, t0=None, T=None, out=None, stream=None):
+        """Several value channels Y (nchan, n) at the same times t, transformed
+        together (shared binning and gridding); returns (nchan, nf)."""
+        if Y.dim() != 2 or Y.shape[1] != t.numel():
+            raise ValueError("Y must be (nchan, n)")
+        t, _, t0, T = self._check(t, Y[0], t0, T)
+        Y = Y.contiguous()
+        if out is None:
+            out = torch.empty((Y.shape[0], self.nf), dtype=self.cdtype, device=t.device)
+        s = (stream if stream is not None else torch.cuda.current_stream(t.device)).cuda_stream
+        _lib.check(_lib.core().cuna2_adjoint_multi(self._h, t.data_ptr(), Y.data_ptr(), out.data_ptr(), t.numel(),
+                                                   Y.shape[0], float(t0), float(T), s or None))
+        return out
+
     def backward(self, t, y, grad_F, t0, T, need_y=True, need_t=True, stream=None):
         """(dL/dy, dL/dt) for grad_F = dL/dRe F + i dL/dIm F (torch's convention)."""
         gy = torch.empty_like(y) if need_y else None

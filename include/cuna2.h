@@ -179,6 +179,24 @@ int cuna2_adjoint(cuna2_plan plan, const double *t, const void *y, void *F, int6
 int cuna2_adjoint_bootstrap(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
                             int nbs, unsigned int seed, double t0, double T, cudaStream_t stream);
 
+/* nchan value channels at the same sample times (y holds nchan rows of n
+ * values, F receives nchan rows of nf outputs), transformed together: one
+ * binning pass and one gridding launch shared by all channels, then one
+ * slab-batched FFT.  A channel of ones gives the window function.
+ * 1 <= nchan <= 65535. */
+int cuna2_adjoint_multi(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
+                        int nchan, double t0, double T, cudaStream_t stream);
+
+/* Generalised (floating-mean) Lomb-Scargle periodogram of (t, y) with
+ * optional uncertainties dy (NULL: equal weights) at frequencies
+ * f_k = (k + 1) df, k < nfreq, written to power (nfreq values of dtype).
+ * Built on one two-channel adjoint NFFT (weighted centred values and
+ * weights) with period 1/df, Nf the smallest power of two > 4 nfreq,
+ * oversampling R and half-width m.  Plans are cached per (device, size). */
+int cuna2_lomb_scargle(int dtype, const double *t, const void *y, const void *dy, int64_t n,
+                       int64_t nfreq, double df, double t0, int R, int m, void *power,
+                       cudaStream_t stream);
+
 /* Vector-Jacobian product of cuna2_adjoint for a real loss L(F): given
  * G[k + nf/2] = dL/dRe F_k + i dL/dIm F_k (nf complex values of the plan's
  * precision), writes dL/dy_j (n values of the plan's precision) to grad_y and
