@@ -19,6 +19,7 @@ SUCCESS = 0
 STATUS = {0: "CUNA2_SUCCESS", 1: "CUNA2_ERROR_INVALID_VALUE", 2: "CUNA2_ERROR_CUDA",
           3: "CUNA2_ERROR_UNSUPPORTED", 4: "CUNA2_ERROR_ALLOC", 5: "CUNA2_ERROR_CUFFT"}
 F32, F64 = 0, 1
+GRID_GATHER, GRID_SCATTER = 0, 1
 
 
 class CunaError(RuntimeError):
@@ -70,6 +71,9 @@ CORE_SIGNATURES = {
     "cuna2_adjoint_multi": (_I, [_P, _P, _P, _P, _I64, _I, _D, _D, _P]),
     "cuna2_lomb_scargle": (_I, [_I, _P, _P, _P, _I64, _I64, _D, _D, _I, _I, _P, _P]),
     "cuna2_plan_set_graph": (_I, [_P, _I]),
+    "cuna2_plan_set_schedule": (_I, [_P, _I, _I]),
+    "cuna2_plan_get_schedule": (_I, [_P, _P, _P]),
+    "cuna2_plan_autotune": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P, _I, _P]),
     "cuna2_plan_profile": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P, _P, _P, _I, _P]),
     "cuna2_batch_plan_create": (_I, [_P, _I, _I, _P, _P, _I, _I, _P, _P]),
     "cuna2_batch_plan_destroy": (_I, [_P]),

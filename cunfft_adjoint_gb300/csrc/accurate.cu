@@ -12,20 +12,26 @@
 // are fused in.
 //
 // Precision: s_j is reduced in 64-bit fixed point (phase.cuh); gridding, FFT
-// and epilogue run in the plan's type.  Float plans use the fast Gaussian
-// gridding factorisation y E1 E2^d E3[d] (E2^d by repeated multiplication).
+// and epilogue run in the plan's type.  The single-CTA path uses the fast
+// Gaussian gridding factorisation y E1 E2^d E3[d] (E2^d by repeated
+// multiplication); the tiled path evaluates each tap (float) or factorises
+// per four taps (double).
 //
 // Kernels:
 //   k_nfft_small<T>      ng <= 2^15 (f32) / 2^14 (f64): one CTA per transform,
 //                        gridding straight into shared memory (no sort), FFT,
 //                        epilogue -- a single launch.
-//   binning (binning.cuh) + k_grid_acc + k_fft_colpass + k_fft_rowpass_acc for
-//                        larger grids.
+//   binning (binning.cuh) + k_grid_scatter / k_grid_acc (the plan's schedule)
+//                        + k_ct_colpass + k_ct_rowpass_acc (fftpass.cuh,
+//                        compile-time geometry per length) for larger grids;
+//                        k_fft_colpass + k_fft_rowpass_acc for lengths without
+//                        a compiled instance.
 #include <math.h>
 #include <algorithm>
 #include <mutex>
 #include <vector>
 #include "accurate_kernels.cuh"
+#include "fftpass.cuh"
 
 struct cuna2_plan_st {
   int dtype;
@@ -33,6 +39,7 @@ struct cuna2_plan_st {
   int R, m;
   double tau;
   int logTL, ntiles;
+  int grid_method = CUNA2_GRID_SCATTER;  // tile gridding form (cuna2_plan_set_schedule)
   bool small;  // single-CTA fused path
   cuna::FftGeom geom;
   int device;
@@ -111,6 +118,46 @@ inline void mark(Prof *pr, const char *name, cudaStream_t st) {
     pr->name[pr->n] = name;
     cudaEventRecord(pr->ev[pr->n++], st);
   }
+}
+
+// Both four-step passes with the compile-time kernels of fftpass.cuh for the
+// lengths that have an instance: returns 1 when launched, 0 when logL has no
+// instance, -1 on a launch error.
+template <typename T, int LOGL>
+int ct_passes_at(typename CxOf<T>::type *z, const FftDev<T> &f, const AccParams<T> &e, typename CxOf<T>::type *F,
+                 int nslab, cudaStream_t st, Prof *pr) {
+  constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
+  constexpr int BA = PassCfg<T>::ELEMS >> LOG1, BB = PassCfg<T>::ELEMS >> LOG2, PB = BB / 2;
+  constexpr int npairs = (1 << LOG1) / 2 + 1;
+  constexpr size_t smA = ct_colpass_smem<T, LOGL>(), smB = ct_rowpass_smem<T, LOGL>();
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(k_ct_colpass<T, LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smA) ||
+        cudaFuncSetAttribute(k_ct_rowpass_acc<T, LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smB))
+      return -1;
+    attr = true;
+  }
+  k_ct_colpass<T, LOGL><<<dim3((1 << LOG2) / BA, nslab), PassCfg<T>::THREADS, smA, st>>>(z, f, (int64_t)1 << LOGL);
+  if (cudaPeekAtLastError() != cudaSuccess) return -1;
+  mark(pr, "fft_colpass", st);
+  k_ct_rowpass_acc<T, LOGL><<<dim3((npairs + PB - 1) / PB, nslab), PassCfg<T>::THREADS, smB, st>>>(z, f, e, F);
+  if (cudaPeekAtLastError() != cudaSuccess) return -1;
+  mark(pr, "fft_rowpass", st);
+  return 1;
+}
+
+template <typename T>
+int ct_passes(int logL, typename CxOf<T>::type *z, const FftDev<T> &f, const AccParams<T> &e,
+              typename CxOf<T>::type *F, int nslab, cudaStream_t st, Prof *pr) {
+#define CUNA_CT(LG) \
+  case LG: return ct_passes_at<T, LG>(z, f, e, F, nslab, st, pr);
+  if constexpr (sizeof(T) == 4) {
+    switch (logL) { CUNA_CT(15) CUNA_CT(16) CUNA_CT(17) CUNA_CT(18) CUNA_CT(19) CUNA_CT(20) CUNA_CT(21) CUNA_CT(22) CUNA_CT(23) CUNA_CT(24) CUNA_CT(25) }
+  } else {
+    switch (logL) { CUNA_CT(14) CUNA_CT(15) CUNA_CT(16) CUNA_CT(17) CUNA_CT(18) CUNA_CT(19) CUNA_CT(20) CUNA_CT(21) CUNA_CT(22) CUNA_CT(23) }
+  }
+#undef CUNA_CT
+  return 0;
 }
 
 // One plan execution.  nbs == 0: a single transform of (t, y).  nbs >= 1:
@@ -199,20 +246,35 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     k_scan_tiles<<<1, 1024, 0, st>>>(counts, offsets, cursor, ntiles);
     CUNA_CK(cudaGetLastError());
   }
-  const size_t smg = grid_smem_bytes<T>(p->logTL, p->m);
-  static bool attr3 = false;
-  if (!attr3) {
-    CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr3 = true;
-  }
-  // bootstrap / channels: each CTA grids a group of slabs of one tile, reusing its sort
+  // bootstrap / channels: each CTA grids a group of slabs of one tile, reusing its staged records
   const int group = wts ? std::min(8, nslab) : 1;
-  k_grid_acc<T><<<dim3(ntiles, (nslab + group - 1) / group), kGridThreads, smg, st>>>(
-      recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+  const dim3 ggrid(ntiles, (nslab + group - 1) / group);
+  if (p->grid_method == CUNA2_GRID_GATHER) {
+    const size_t smg = grid_smem_bytes<T>(p->logTL, p->m);
+    static bool attr3 = false;
+    if (!attr3) {
+      CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      attr3 = true;
+    }
+    k_grid_acc<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+  } else {
+    const size_t smg = grid_scatter_smem_bytes<T>(p->logTL);
+    static bool attr4 = false;
+    if (!attr4) {
+      CUNA_CK(cudaFuncSetAttribute(k_grid_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      attr4 = true;
+    }
+    k_grid_scatter<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+  }
   CUNA_CK(cudaGetLastError());
   mark(pr, "grid", st);
   // packed complex view of the real grid slabs
   C *z = reinterpret_cast<C *>(grid);
+  {
+    const int h = ct_passes<T>(p->geom.logL, z, f, e, F, nslab, st, pr);
+    if (h < 0) return fail_cuda(cudaGetLastError(), "FFT pass launch");
+    if (h == 1) return CUNA2_SUCCESS;
+  }
   const int elems = sizeof(T) == 4 ? kPassElemsF32 : kPassElemsF64;
   const int threads = elems / kFftE;
   const int L1 = 1 << p->geom.logL1, L2 = 1 << p->geom.logL2;
@@ -417,6 +479,106 @@ extern "C" int cuna2_plan_profile(cuna2_plan p, const double *t, const void *y, 
   *nstages = k;
   for (int i = 0; i < 16; ++i) cudaEventDestroy(pr.ev[i]);
   return s;
+}
+
+namespace cuna {
+namespace {
+bool schedule_ok(const cuna2_plan_st *p, int log_tile, int method) {
+  const int logng = ilog2i(p->ng);
+  if (method != CUNA2_GRID_GATHER && method != CUNA2_GRID_SCATTER) return false;
+  if (log_tile < 2 || log_tile > logng || log_tile > (method == CUNA2_GRID_GATHER ? 12 : 13)) return false;
+  // with more than one tile a record's 2m taps must touch at most two tiles
+  return log_tile == logng || (1 << log_tile) >= 2 * p->m;
+}
+void drop_graphs(cuna2_plan_st *p) {
+  for (auto &g : p->graphs) cudaGraphExecDestroy(g.exec);
+  p->graphs.clear();
+}
+}  // namespace
+}  // namespace cuna
+
+extern "C" int cuna2_plan_set_schedule(cuna2_plan p, int log_tile, int grid_method) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (!schedule_ok(p, log_tile, grid_method))
+    return fail(CUNA2_ERROR_INVALID_VALUE, "schedule (log_tile=%d, grid_method=%d) not admissible for ng=%lld m=%d",
+                log_tile, grid_method, (long long)p->ng, p->m);
+  if (log_tile != p->logTL || grid_method != p->grid_method) drop_graphs(p);
+  p->logTL = log_tile;
+  p->ntiles = (int)(p->ng >> log_tile);
+  p->grid_method = grid_method;
+  return CUNA2_SUCCESS;
+}
+
+extern "C" int cuna2_plan_get_schedule(cuna2_plan p, int *log_tile, int *grid_method) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  if (log_tile) *log_tile = p->logTL;
+  if (grid_method) *grid_method = p->grid_method;
+  return CUNA2_SUCCESS;
+}
+
+// Time `reps` plain runs of the current schedule on `st` (min over runs).
+static int time_schedule(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0, double T,
+                         cudaStream_t st, int reps, float *ms) {
+  cudaEvent_t a, b;
+  CUNA_CK(cudaEventCreate(&a));
+  CUNA_CK(cudaEventCreate(&b));
+  int s = run_any(p, t, y, F, n, t0, T, st, nullptr);  // warm-up; grows the workspace
+  float best = 3.4e38f;
+  for (int r = 0; !s && r < reps; ++r) {
+    cudaEventRecord(a, st);
+    s = run_any(p, t, y, F, n, t0, T, st, nullptr);
+    cudaEventRecord(b, st);
+    if (!s) {
+      cudaError_t e = cudaEventSynchronize(b);
+      if (e != cudaSuccess) s = fail_cuda(e, "cudaEventSynchronize");
+    }
+    float x = 0;
+    if (!s) cudaEventElapsedTime(&x, a, b);
+    best = std::min(best, x);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms = best;
+  return s;
+}
+
+extern "C" int cuna2_plan_autotune(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0,
+                                   double T, cudaStream_t st, int reps, float *best_ms) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  if (reps < 1) reps = 5;
+  std::lock_guard<std::mutex> lk(p->mu);
+  const int logng = ilog2i(p->ng);
+  int best_tile = p->logTL, best_method = p->grid_method;
+  float best = 3.4e38f;
+  if (p->small) {  // one fused CTA per transform: no tiles to choose
+    CUNA_TRY(time_schedule(p, t, y, F, n, t0, T, st, reps, &best));
+  } else {
+    for (int method = CUNA2_GRID_GATHER; method <= CUNA2_GRID_SCATTER; ++method)
+      for (int lt = 9; lt <= 13; ++lt) {
+        if (!schedule_ok(p, lt, method) || lt == logng) continue;
+        drop_graphs(p);
+        p->logTL = lt;
+        p->ntiles = (int)(p->ng >> lt);
+        p->grid_method = method;
+        float ms = 0;
+        CUNA_TRY(time_schedule(p, t, y, F, n, t0, T, st, reps, &ms));
+        if (ms < best) {
+          best = ms;
+          best_tile = lt;
+          best_method = method;
+        }
+      }
+    drop_graphs(p);
+    p->logTL = best_tile;
+    p->ntiles = (int)(p->ng >> best_tile);
+    p->grid_method = best_method;
+  }
+  if (best_ms) *best_ms = best;
+  return CUNA2_SUCCESS;
 }
 
 extern "C" int cuna2_adjoint_bootstrap(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, int nbs,

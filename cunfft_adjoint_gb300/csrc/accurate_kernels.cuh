@@ -19,6 +19,7 @@
 #pragma once
 #include <math.h>
 #include <algorithm>
+#include <type_traits>
 #include "binning.cuh"
 #include "fft.cuh"
 #include "phase.cuh"
@@ -223,9 +224,62 @@ __device__ __forceinline__ float ex2_fast(float x) {
 __device__ __forceinline__ float gauss_w(float y, float dd, float k1) { return y * ex2_fast(-k1 * dd * dd); }
 __device__ __forceinline__ double gauss_w(double y, double dd, double k1) { return y * exp2(-k1 * dd * dd); }
 
-template <typename T> struct Pair;
-template <> struct Pair<float> { typedef float2 type; };
-template <> struct Pair<double> { typedef double2 type; };
+// a placed record in shared memory: fractional cell, value, slot
+template <typename T> struct __align__(2 * sizeof(T) >= 16 ? 16 : 16) SRec {
+  T f, y;
+  int lc, pad;
+};
+constexpr int kGridCW = 4;  // consecutive cells per thread in the gather
+
+// Weights y exp2(-k1 (x + i)^2) of one record for four consecutive cells,
+// i = 0..3.  float: four ex2.approx.  double: the fast Gaussian gridding
+// factorisation (Greengard & Lee 2004) exp2(-k1 (x+i)^2) = E Q^i c_i with
+// E = exp2(-k1 x^2), Q = exp2(-2 k1 x), c_i = exp2(-k1 i^2): two exp2 per
+// record instead of four, the FP64 pipe being the bound of the double path.
+template <typename T> struct Gauss4;
+template <> struct Gauss4<float> {
+  __device__ explicit Gauss4(float) {}
+};
+template <> struct Gauss4<double> {
+  double c1, c2, c3;
+  __device__ explicit Gauss4(double k1) : c1(exp2(-k1)), c2(exp2(-4.0 * k1)), c3(exp2(-9.0 * k1)) {}
+};
+__device__ __forceinline__ void gauss_w4(float y, float x, float k1, const Gauss4<float> &, float &w0, float &w1,
+                                         float &w2, float &w3) {
+  w0 = gauss_w(y, x, k1);
+  w1 = gauss_w(y, x + 1.f, k1);
+  w2 = gauss_w(y, x + 2.f, k1);
+  w3 = gauss_w(y, x + 3.f, k1);
+}
+__device__ __forceinline__ void gauss_w4(double y, double x, double k1, const Gauss4<double> &g, double &w0,
+                                         double &w1, double &w2, double &w3) {
+  const double E = y * exp2(-k1 * x * x), Q = exp2(-2.0 * k1 * x);
+  const double t1 = E * Q, t2 = t1 * Q, t3 = t2 * Q;
+  w0 = E;
+  w1 = t1 * g.c1;
+  w2 = t2 * g.c2;
+  w3 = t3 * g.c3;
+}
+
+__device__ __forceinline__ void store4(float *p, float a, float b, float c, float d) {
+  *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void store4(double *p, double a, double b, double c, double d) {
+  reinterpret_cast<double2 *>(p)[0] = make_double2(a, b);
+  reinterpret_cast<double2 *>(p)[1] = make_double2(c, d);
+}
+
+// Slots (local cell + m) of a record whose cell is p0 cells right of the tile
+// base, for every image p = p0 + j*ng (j in {-1, 0, 1}) in [-m, TL + m); the
+// second slot exists only when one tile spans the whole periodic grid.
+__device__ __forceinline__ void grid_slots(int p0, int ng, int TL, int m, int &s0, int &s1) {
+  if (p0 < 0) p0 += ng;
+  const int a = p0 - ng >= -m ? p0 - ng + m : -1;
+  const int b = p0 < TL + m ? p0 + m : -1;
+  const int c = p0 + ng < TL + m ? p0 + ng + m : -1;
+  s0 = a >= 0 ? a : (b >= 0 ? b : c);
+  s1 = a >= 0 ? (b >= 0 ? b : c) : (b >= 0 ? c : -1);
+}
 
 // One grid tile [base, base + 2^logTL) from records [r0, r1), for slabs
 // [sbeg, send): slab s grids value wts[s*nvals + p] of sample p when wts is
@@ -236,22 +290,22 @@ __device__ __forceinline__ void grid_tile_body(const typename RecOf<T>::type *__
                                                const T *__restrict__ wts, int64_t nvals, int sbeg, int send,
                                                int64_t slab_stride) {
   typedef typename RecOf<T>::type Rec;
-  typedef typename Pair<T>::type P2;
   constexpr int CAP = GridCfg<T>::CAP;
   constexpr int RPT = CAP / kGridThreads;  // records per thread per chunk
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int TL = 1 << e.logTL, m = e.m, W = TL + 2 * m;
   const int ng = (int)e.ng;
-  int *start = reinterpret_cast<int *>(smem_raw);                                   // W + 1 slots
-  P2 *sfy = reinterpret_cast<P2 *>(smem_raw + sizeof(int) * ((W + 2 + 3) & ~3));  // (frac, value)
-  int *sp = reinterpret_cast<int *>(sfy + CAP);                                    // sample index
-  short *slc = reinterpret_cast<short *>(sp + CAP);                                // slot
+  int *start = reinterpret_cast<int *>(smem_raw);                                       // W + 1 slots
+  SRec<T> *srec = reinterpret_cast<SRec<T> *>(smem_raw + sizeof(int) * ((W + 2 + 3) & ~3));  // placed records
+  int *sp = reinterpret_cast<int *>(srec + CAP);                                         // sample index
   __shared__ int wsum[kGridThreads / 32];
   // a single tile spanning the whole grid maps a record to up to two slots;
   // halve the chunk then so that placements never exceed CAP
   const int chunk = (TL + 2 * m > ng) ? CAP / 2 : CAP;
-  const int cpt = (TL + kGridThreads - 1) / kGridThreads;
+  const int npass = (TL + kGridThreads * kGridCW - 1) / (kGridThreads * kGridCW);  // <= kGridMaxCpt / kGridCW
   const int nchunks = (r1 - r0 + chunk - 1) / chunk;
+  const Gauss4<T> g4(e.k1);
+  // the records are sorted once for all slabs when they fit in one chunk
   for (int slab = sbeg; slab < send; ++slab) {
     T acc[kGridMaxCpt];
 #pragma unroll
@@ -265,7 +319,6 @@ __device__ __forceinline__ void grid_tile_body(const typename RecOf<T>::type *__
         // load this thread's records; each maps to up to two slots (two only
         // when the tile wraps onto itself, i.e. one tile spans the whole grid)
         Rec rc[RPT];
-        int sl[RPT][2];
 #pragma unroll
         for (int u = 0; u < RPT; ++u) {
           const int i = threadIdx.x + u * kGridThreads;
@@ -274,18 +327,11 @@ __device__ __forceinline__ void grid_tile_body(const typename RecOf<T>::type *__
 #pragma unroll
         for (int u = 0; u < RPT; ++u) {
           const int i = threadIdx.x + u * kGridThreads;
-          sl[u][0] = sl[u][1] = -1;
           if (i < cnt) {
-            int p0 = rc[u].cell - base;
-            if (p0 < 0) p0 += ng;
-            // slots p + m for every p = p0 + j*ng in [-m, TL + m), j in {-1, 0, 1}
-            const int a = p0 - ng >= -m ? p0 - ng + m : -1;
-            const int b = p0 < TL + m ? p0 + m : -1;
-            const int c = p0 + ng < TL + m ? p0 + ng + m : -1;
-            sl[u][0] = a >= 0 ? a : (b >= 0 ? b : c);
-            sl[u][1] = a >= 0 ? (b >= 0 ? b : c) : (b >= 0 ? c : -1);
-            if (sl[u][0] >= 0) atomicAdd(&start[sl[u][0]], 1);
-            if (sl[u][1] >= 0) atomicAdd(&start[sl[u][1]], 1);
+            int s0, s1;
+            grid_slots(rc[u].cell - base, ng, TL, m, s0, s1);
+            if (s0 >= 0) atomicAdd(&start[s0], 1);
+            if (s1 >= 0) atomicAdd(&start[s1], 1);
           }
         }
         __syncthreads();
@@ -325,17 +371,22 @@ __device__ __forceinline__ void grid_tile_body(const typename RecOf<T>::type *__
         // place: afterwards start[lc] is the END of slot lc
 #pragma unroll
         for (int u = 0; u < RPT; ++u) {
+          const int i = threadIdx.x + u * kGridThreads;
+          if (i >= cnt) continue;
+          int sl[2];
+          grid_slots(rc[u].cell - base, ng, TL, m, sl[0], sl[1]);
 #pragma unroll
           for (int q = 0; q < 2; ++q) {
-            const int lc = sl[u][q];
+            const int lc = sl[q];
             if (lc < 0) continue;
             const int pos = atomicAdd(&start[lc], 1);
-            P2 fy;
-            fy.x = rc[u].a;
-            fy.y = rc[u].b;
-            sfy[pos] = fy;
+            SRec<T> r;
+            r.f = rc[u].a;
+            r.y = rc[u].b;
+            r.lc = lc;
+            r.pad = 0;
+            srec[pos] = r;
             sp[pos] = rc[u].p;
-            slc[pos] = (short)lc;
           }
         }
         __syncthreads();
@@ -343,32 +394,49 @@ __device__ __forceinline__ void grid_tile_body(const typename RecOf<T>::type *__
       if (wts) {  // this slab's values for the placed records
         const int placed = start[W - 1];
         const T *ws = wts + (int64_t)slab * nvals;
-        for (int i = threadIdx.x; i < placed; i += kGridThreads) sfy[i].y = ws[sp[i]];
+        for (int i = threadIdx.x; i < placed; i += kGridThreads) srec[i].y = ws[sp[i]];
         __syncthreads();
       }
-      // gather: cell c_l (local) takes slots c_l .. c_l + 2m - 1
+      // gather: the thread's cells cl0 .. cl0+3 (local) take the records in
+      // slots cl0 .. cl0 + 3 + 2m - 1; record slot lc reaches cell c iff
+      // 0 <= lc - c < 2m
 #pragma unroll
-      for (int q = 0; q < kGridMaxCpt; ++q) {
-        const int cl = threadIdx.x + q * kGridThreads;
-        if (q >= cpt || cl >= TL) continue;
-        const int rb = cl == 0 ? 0 : start[cl - 1];
-        const int re = start[cl + 2 * m - 1];
-        T a = (T)0;
-        const int ctr = cl + m;
-#pragma unroll 2
+      for (int q = 0; q < kGridMaxCpt / kGridCW; ++q) {
+        const int cl0 = (threadIdx.x + q * kGridThreads) * kGridCW;
+        if (q >= npass || cl0 >= TL) continue;
+        const int rb = cl0 == 0 ? 0 : start[cl0 - 1];
+        const int re = start[cl0 + kGridCW - 1 + 2 * m - 1];
+        T a0 = (T)0, a1 = (T)0, a2 = (T)0, a3 = (T)0;
+        const int ctr = cl0 + m;
         for (int r = rb; r < re; ++r) {
-          const P2 fy = sfy[r];
-          const T dd = (T)(ctr - (int)slc[r]) - fy.x;
-          a += gauss_w(fy.y, dd, e.k1);
+          const SRec<T> rr = srec[r];
+          const int rel = rr.lc - cl0;                 // lc - c for c = cl0
+          const T dd0 = (T)(ctr - rr.lc) - rr.f;       // d - f for c = cl0
+          const unsigned w2 = (unsigned)(2 * m);
+          T w0, w1, wq2, w3;
+          gauss_w4(rr.y, dd0, e.k1, g4, w0, w1, wq2, w3);
+          a0 += (unsigned)rel < w2 ? w0 : (T)0;
+          a1 += (unsigned)(rel - 1) < w2 ? w1 : (T)0;
+          a2 += (unsigned)(rel - 2) < w2 ? wq2 : (T)0;
+          a3 += (unsigned)(rel - 3) < w2 ? w3 : (T)0;
         }
-        acc[q] += a;
+        acc[4 * q + 0] += a0;
+        acc[4 * q + 1] += a1;
+        acc[4 * q + 2] += a2;
+        acc[4 * q + 3] += a3;
       }
       __syncthreads();
     }
     T *out = grid + (int64_t)slab * slab_stride + base;
 #pragma unroll
-    for (int q = 0; q < kGridMaxCpt; ++q)
-      if (q < cpt && threadIdx.x + q * kGridThreads < TL) out[threadIdx.x + q * kGridThreads] = acc[q];
+    for (int q = 0; q < kGridMaxCpt / kGridCW; ++q) {
+      const int cl0 = (threadIdx.x + q * kGridThreads) * kGridCW;
+      // TL is a power of two >= 4 (ng >= 4m >= 4), so every group of four
+      // cells is whole and the vector store stays inside the tile
+      if (q < npass && cl0 < TL) {
+        store4(out + cl0, acc[4 * q + 0], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+      }
+    }
   }
 }
 
@@ -383,10 +451,91 @@ __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 4 : 2) k_grid_a
                     slab_stride);
 }
 
+// Scatter form of the same tile gridding: the tile's cells accumulate in
+// shared memory, one thread per (record, tap) pair adds its Gaussian weight
+// with a shared-memory atomic, and the tile is flushed to HBM once, in cell
+// order, with vector stores (no global atomics).  A block step covers
+// floor(256 / 2m) records, thread t taking tap t mod 2m of record t / 2m, so
+// every lane of a warp does useful work whatever the record density.  A tap
+// lands in cell (cell + d) mod ng, kept when it falls in this tile; ng is a
+// power of two.  Summation order within a cell follows the atomics.
+template <typename T>
+__device__ __forceinline__ void grid_tile_scatter(const typename RecOf<T>::type *__restrict__ recs, int r0, int r1,
+                                                  int base, T *__restrict__ grid, const AccParams<T> &e,
+                                                  const T *__restrict__ wts, int64_t nvals, int sbeg, int send,
+                                                  int64_t slab_stride) {
+  typedef typename RecOf<T>::type Rec;
+  constexpr int CAP = GridCfg<T>::CAP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int TL = 1 << e.logTL, m = e.m, W2 = 2 * m;
+  const int gmask = (int)e.ng - 1;
+  T *acc = reinterpret_cast<T *>(smem_raw);                          // TL cells
+  SRec<T> *srec = reinterpret_cast<SRec<T> *>(smem_raw + sizeof(T) * TL);  // CAP staged records
+  int *sp = reinterpret_cast<int *>(srec + CAP);                       // sample index (weights)
+  const int per = kGridThreads / W2;  // records per block step (W2 <= 32)
+  const int rr = threadIdx.x / W2;
+  const int d = (int)threadIdx.x - rr * W2 - m + 1;  // tap offset in [-m+1, m]
+  const T dT = (T)d;
+  const bool active = rr < per;
+  const int nchunks = (r1 - r0 + CAP - 1) / CAP;
+  for (int slab = sbeg; slab < send; ++slab) {
+    for (int i = 4 * threadIdx.x; i < TL; i += 4 * kGridThreads) store4(acc + i, (T)0, (T)0, (T)0, (T)0);
+    for (int ck = 0; ck < nchunks; ++ck) {
+      const int c0 = r0 + ck * CAP;
+      const int cnt = min(CAP, r1 - c0);
+      if (nchunks > 1 || slab == sbeg) {
+        for (int i = threadIdx.x; i < cnt; i += kGridThreads) {
+          const Rec rc = recs[c0 + i];
+          SRec<T> r;
+          r.f = rc.a;
+          r.y = rc.b;
+          r.lc = rc.cell - base;
+          r.pad = 0;
+          srec[i] = r;
+          sp[i] = rc.p;
+        }
+      }
+      if (wts) {
+        __syncthreads();
+        const T *ws = wts + (int64_t)slab * nvals;
+        for (int i = threadIdx.x; i < cnt; i += kGridThreads) srec[i].y = ws[sp[i]];
+      }
+      __syncthreads();
+      if (active) {
+        for (int r = rr; r < cnt; r += per) {
+          const SRec<T> q = srec[r];
+          const int lc = (q.lc + d) & gmask;
+          const T w = gauss_w(q.y, dT - q.f, e.k1);
+          if (lc < TL) atomicAdd(&acc[lc], w);
+        }
+      }
+      __syncthreads();
+    }
+    // fixed-order flush; TL is a power of two >= 4, so groups of four are whole
+    T *out = grid + (int64_t)slab * slab_stride + base;
+    for (int i = 4 * threadIdx.x; i < TL; i += 4 * kGridThreads) store4(out + i, acc[i], acc[i + 1], acc[i + 2], acc[i + 3]);
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 3) k_grid_scatter(
+    const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
+    AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab, int group, int64_t slab_stride) {
+  const int tile = blockIdx.x;
+  const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
+  grid_tile_scatter<T>(recs, off[tile], off[tile + 1], tile << e.logTL, grid, e, wts, nvals, sbeg, send,
+                       slab_stride);
+}
+
+template <typename T> size_t grid_scatter_smem_bytes(int logTL) {
+  return sizeof(T) * ((size_t)1 << logTL) + (sizeof(SRec<T>) + sizeof(int)) * (size_t)GridCfg<T>::CAP;
+}
+
 template <typename T> size_t grid_smem_bytes(int logTL, int m) {
   const int W = (1 << logTL) + 2 * m;
   const size_t CAP = GridCfg<T>::CAP;
-  return sizeof(int) * ((W + 2 + 3) & ~3) + sizeof(T) * 2 * CAP + sizeof(int) * CAP + sizeof(short) * CAP;
+  return sizeof(int) * ((W + 2 + 3) & ~3) + sizeof(SRec<T>) * CAP + sizeof(int) * CAP;
 }
 
 // Last four-step pass of the packed real transform: CTA owns row pairs

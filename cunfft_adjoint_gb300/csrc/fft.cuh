@@ -31,7 +31,7 @@ __device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
 // `nseq` sequences are stored side by side: at least L + L/16, and congruent
 // to 16/nseq (mod 16) so that the column-wise global<->shared copies of the
 // four-step passes spread over all banks.
-__host__ __device__ __forceinline__ int fft_pitch(int L, int nseq) {
+__host__ __device__ constexpr int fft_pitch(int L, int nseq) {
   int base = L + (L >> 4) + 1;
   int want = nseq >= 16 ? 1 : 16 / (nseq > 0 ? nseq : 1);
   int r = base & 15;

@@ -105,6 +105,28 @@ class AdjointNFFT:
             None if gt is None else gt.data_ptr(), t.numel(), float(t0), float(T), s or None))
         return gy, gt
 
+    @property
+    def schedule(self):
+        """(log_tile, grid_method) of the tiled gridding."""
+        lt, gm = ctypes.c_int(), ctypes.c_int()
+        _lib.check(_lib.core().cuna2_plan_get_schedule(self._h, ctypes.byref(lt), ctypes.byref(gm)))
+        return lt.value, gm.value
+
+    def set_schedule(self, log_tile, grid_method):
+        """Tiles of 2**log_tile cells, gridded in GRID_GATHER or GRID_SCATTER form."""
+        _lib.check(_lib.core().cuna2_plan_set_schedule(self._h, int(log_tile), int(grid_method)))
+
+    def autotune(self, t, y, t0=None, T=None, reps=5, stream=None):
+        """Time every admissible schedule on (t, y), keep the fastest; returns
+        (log_tile, grid_method, best_ms)."""
+        t, y, t0, T = self._check(t, y, t0, T)
+        out = torch.empty(self.nf, dtype=self.cdtype, device=t.device)
+        s = (stream if stream is not None else torch.cuda.current_stream(t.device)).cuda_stream
+        ms = ctypes.c_float()
+        _lib.check(_lib.core().cuna2_plan_autotune(self._h, t.data_ptr(), y.data_ptr(), out.data_ptr(), t.numel(),
+                                                   float(t0), float(T), s or None, int(reps), ctypes.byref(ms)))
+        return self.schedule + (ms.value,)
+
     def frequencies(self):
         """Integer frequency index k of each output bin."""
         return torch.arange(-self.nf // 2, self.nf // 2, dtype=torch.int64)

@@ -228,6 +228,30 @@ int cuna2_plan_profile(cuna2_plan plan, const double *t, const void *y, void *F,
                        double t0, double T, cudaStream_t stream, float *stage_ms,
                        const char **stage_names, int max_stages, int *nstages);
 
+/* Gridding schedule.  The grid is cut into tiles of 2^log_tile cells, one CTA
+ * per tile staging it in shared memory and writing it to HBM once.  Forms:
+ *   CUNA2_GRID_GATHER   the tile's records are counting-sorted by cell in
+ *                       shared memory and each thread sums four consecutive
+ *                       cells over its window of records (log_tile <= 12);
+ *   CUNA2_GRID_SCATTER  one thread per (record, tap) adds its Gaussian weight
+ *                       into the shared tile (log_tile <= 13).
+ * Both compute the same sums.  With more than one tile, 2^log_tile >= 2m.
+ * New plans start at (min(log2 ng, 12), CUNA2_GRID_SCATTER).  Changing the
+ * schedule drops the plan's cached graphs.  No counterpart in the reference
+ * (its gridding kernel, src/gridding.cu:36-65, has a fixed launch shape). */
+enum { CUNA2_GRID_GATHER = 0, CUNA2_GRID_SCATTER = 1 };
+int cuna2_plan_set_schedule(cuna2_plan plan, int log_tile, int grid_method);
+int cuna2_plan_get_schedule(cuna2_plan plan, int *log_tile, int *grid_method);
+
+/* Autotuner: runs the transform of (t, y) into F under every admissible
+ * schedule with log_tile in 9..13 (below the whole grid), reps timed runs
+ * each (CUDA events on `stream`, minimum taken), and keeps the fastest;
+ * best_ms (may be NULL) receives its time.  Synchronises `stream`.  Plans
+ * small enough for the single-CTA path have nothing to tune and keep their
+ * schedule. */
+int cuna2_plan_autotune(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
+                        double t0, double T, cudaStream_t stream, int reps, float *best_ms);
+
 /* ---------------------------------------------------------------------- */
 /* batched accurate mode: many series of uneven length                     */
 /* ---------------------------------------------------------------------- */

@@ -124,3 +124,97 @@ def test_plan_errors(nfft):
         nfft.AdjointNFFT(1000, 3, 8)   # R*nf/2 not a power of two
     with pytest.raises(CunaError):
         nfft.AdjointNFFT(1024, 2, 40)  # m out of range
+
+
+SCHED_CASES = [
+    # n, nf, R, m, dtype, tol vs NDFT      (four-step path: tiles in use)
+    (150_000, 1 << 16, 2, 8, torch.float32, 1e-5),
+    (60_000, 1 << 15, 4, 12, torch.float64, 1e-11),
+]
+
+
+@pytest.mark.parametrize("n,nf,R,m,dtype,tol", SCHED_CASES)
+def test_every_schedule(nfft, oracle_lib, n, nf, R, m, dtype, tol):
+    """Both gridding forms at every admissible tile size give the NDFT's
+    spectrum; the two forms agree with each other to rounding."""
+    from cunfft_adjoint_gb300 import _lib
+    rng = np.random.default_rng(n)
+    t = rng.uniform(0, 500.0, n)
+    y = rng.normal(0, 1, n).astype(np.float32 if dtype == torch.float32 else np.float64)
+    td = torch.as_tensor(t, device="cuda")
+    yd = torch.as_tensor(y, dtype=dtype, device="cuda")
+    plan = nfft.AdjointNFFT(nf, R, m, dtype)
+    k = np.arange(-nf // 2, nf // 2)
+    sel = np.sort(rng.choice(k, 256, replace=False))
+    D = oracle_lib.ndft(t, y.astype(np.float64), 0.0, 500.0, sel)
+    outs = {}
+    for gm in (_lib.GRID_GATHER, _lib.GRID_SCATTER):
+        for lt in (9, 10, 11, 12, 13):
+            if gm == _lib.GRID_GATHER and lt == 13:
+                with pytest.raises(_lib.CunaError):
+                    plan.set_schedule(lt, gm)
+                continue
+            plan.set_schedule(lt, gm)
+            assert plan.schedule == (lt, gm)
+            F = plan(td, yd, 0.0, 500.0).cpu().numpy().astype(np.complex128)
+            assert rel_l2(F[sel + nf // 2], D) < tol, (lt, gm)
+            outs[(lt, gm)] = F
+    ref = outs[(12, _lib.GRID_GATHER)]
+    for key, F in outs.items():
+        assert rel_l2(F, ref) < (2e-6 if dtype == torch.float32 else 1e-13), key
+
+
+def test_schedule_rejects_bad_values(nfft):
+    from cunfft_adjoint_gb300 import _lib
+    plan = nfft.AdjointNFFT(1 << 16, 2, 16, torch.float32)
+    for lt, gm in ((4, _lib.GRID_SCATTER), (14, _lib.GRID_SCATTER), (12, 7), (1, _lib.GRID_GATHER)):
+        with pytest.raises(_lib.CunaError):
+            plan.set_schedule(lt, gm)
+    assert plan.schedule == (12, _lib.GRID_SCATTER)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_schedules_with_slab_weights(nfft, oracle_lib, dtype):
+    """Bootstrap and multi-channel transforms (per-slab weights) under both
+    gridding forms match each other and the per-resample transforms."""
+    from cunfft_adjoint_gb300 import _lib
+    rng = np.random.default_rng(3)
+    n, nf, R, m = 5000, 1 << 14, 4, 8
+    t = rng.uniform(0, 100.0, n)
+    y = rng.normal(0, 1, n)
+    td = torch.as_tensor(t, device="cuda")
+    yd = torch.as_tensor(y, dtype=dtype, device="cuda")
+    Y = torch.stack([yd, yd * 0 + 1, yd * yd])
+    plan = nfft.AdjointNFFT(nf, R, m, dtype)
+    res = []
+    for gm in (_lib.GRID_GATHER, _lib.GRID_SCATTER):
+        plan.set_schedule(11, gm)
+        B = plan.bootstrap(td, yd, 40, 17, 0.0, 100.0).cpu().numpy()
+        M = plan.multi(td, Y, 0.0, 100.0).cpu().numpy()
+        res.append((B, M))
+    tol = 2e-6 if dtype == torch.float32 else 1e-13
+    assert rel_l2(res[0][0], res[1][0]) < tol
+    assert rel_l2(res[0][1], res[1][1]) < tol
+    D = oracle_lib.ndft(t, np.ones(n), 0.0, 100.0, np.arange(-nf // 2, nf // 2)[::64])
+    # m = 8, R = 4: Gaussian kernel accuracy about exp(-pi m sqrt(1 - 1/R)) = 3.5e-10
+    assert rel_l2(res[1][1][1][::64], D) < (1e-5 if dtype == torch.float32 else 2e-9)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_autotune(nfft, oracle_lib, dtype):
+    from cunfft_adjoint_gb300 import _lib
+    rng = np.random.default_rng(11)
+    n, nf = 300_000, 1 << 18
+    t = rng.uniform(0, 1000.0, n)
+    y = rng.normal(0, 1, n)
+    td = torch.as_tensor(t, device="cuda")
+    yd = torch.as_tensor(y, dtype=dtype, device="cuda")
+    plan = nfft.AdjointNFFT(nf, 2, 8, dtype)
+    lt, gm, ms = plan.autotune(td, yd, 0.0, 1000.0, reps=3)
+    assert 9 <= lt <= 13 and gm in (_lib.GRID_GATHER, _lib.GRID_SCATTER) and ms > 0
+    assert plan.schedule == (lt, gm)
+    F = plan(td, yd, 0.0, 1000.0).cpu().numpy().astype(np.complex128)
+    sel = np.sort(rng.choice(np.arange(-nf // 2, nf // 2), 128, replace=False))
+    D = oracle_lib.ndft(t, y, 0.0, 1000.0, sel)
+    # m = 8, R = 2: Gaussian kernel accuracy about exp(-pi m sqrt(1 - 1/R)) = 1.9e-8
+    assert rel_l2(F[sel + nf // 2], D) < (1e-5 if dtype == torch.float32 else 5e-8)
