@@ -145,9 +145,9 @@ def stage_bytes(n, ng, nf, rec_bytes=16, elem=4):
     L = ng // 2
     c = 2 * elem
     return {
-        "bin_count": 8 * n,                                  # read t
+        "bin_count": 16 * n,                                 # read t; write the 64-bit phases
         "scan_tiles": 0,
-        "bin_scatter": 8 * n + elem * n + rec_bytes * n,     # read t, y; write records
+        "bin_scatter": 8 * n + elem * n + rec_bytes * n,     # read phases, y; write records
         "grid": rec_bytes * n + elem * ng,                    # read records; write real grid
         "fft_colpass": 2 * c * L,                            # read + write the packed grid
         "fft_rowpass": c * L + c * nf,                       # read packed grid; write F

@@ -19,7 +19,7 @@ SUCCESS = 0
 STATUS = {0: "CUNA2_SUCCESS", 1: "CUNA2_ERROR_INVALID_VALUE", 2: "CUNA2_ERROR_CUDA",
           3: "CUNA2_ERROR_UNSUPPORTED", 4: "CUNA2_ERROR_ALLOC", 5: "CUNA2_ERROR_CUFFT"}
 F32, F64 = 0, 1
-GRID_GATHER, GRID_SCATTER = 0, 1
+GRID_GATHER, GRID_SCATTER, GRID_FIXED = 0, 1, 2
 
 
 class CunaError(RuntimeError):

@@ -39,7 +39,7 @@ struct cuna2_plan_st {
   int R, m;
   double tau;
   int logTL, ntiles;
-  int grid_method = CUNA2_GRID_SCATTER;  // tile gridding form (cuna2_plan_set_schedule)
+  int grid_method = CUNA2_GRID_GATHER;  // tile gridding form (cuna2_plan_set_schedule)
   bool small;  // single-CTA fused path
   cuna::FftGeom geom;
   int device;
@@ -186,9 +186,10 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   const FftDev<T> f = to_dev<T>(p->geom);
   const int L = 1 << p->geom.logL;
   const int ntiles = p->ntiles;
-  // workspace: counts | offsets | cursor | records | grid slabs | weights
-  const size_t o_cnt = 0, o_off = align_up(sizeof(int) * ntiles), o_cur = o_off + align_up(sizeof(int) * (ntiles + 1));
-  const size_t o_rec = o_cur + align_up(sizeof(int) * ntiles);
+  // workspace: counts | cursor | offsets | phases | records | grid slabs | weights
+  const size_t o_cnt = 0, o_cur = align_up(sizeof(int) * ntiles), o_off = 2 * o_cur;
+  const size_t o_phs = o_off + align_up(sizeof(int) * (ntiles + 1));
+  const size_t o_rec = o_phs + (p->small ? 0 : align_up(sizeof(uint64_t) * (size_t)(n > 0 ? n : 1)));
   const size_t o_grid = o_rec + (p->small ? 0 : align_up(sizeof(Rec) * 2 * (size_t)(n > 0 ? n : 1)));
   const size_t o_wts = o_grid + (p->small ? 0 : align_up(sizeof(T) * (size_t)p->ng * nslab));
   const size_t bytes = o_wts + (nbs > 0 ? sizeof(T) * (size_t)n * nbs : 0) + 256;
@@ -196,6 +197,7 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   CUNA_TRY(plan_workspace(p, bytes, &ws));
   char *w = (char *)ws;
   int *counts = (int *)(w + o_cnt), *offsets = (int *)(w + o_off), *cursor = (int *)(w + o_cur);
+  uint64_t *phases = (uint64_t *)(w + o_phs);
   Rec *recs = (Rec *)(w + o_rec);
   T *grid = (T *)(w + o_grid);
   T *wts = multi ? const_cast<T *>(multi) : (nbs > 0 ? (T *)(w + o_wts) : nullptr);
@@ -226,12 +228,34 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     mark(pr, "nfft_small", st);
     return CUNA2_SUCCESS;
   }
-  CUNA_CK(cudaMemsetAsync(counts, 0, sizeof(int) * ntiles, st));
-  if (n > 0) {
+  // counts and cursor are adjacent: one memset zeroes both
+  CUNA_CK(cudaMemsetAsync(counts, 0, o_off, st));
+  if (n > 0 && ntiles <= kScanFuseTiles) {
+    // count (caching each sample's phase), then scan + scatter in one launch
+    SampAcc<T> smp{t, y, n, pm, e, phases};
+    SampAccS<T> sms{phases, y, n, e};
+    const int nsm = device_sm_count();
+    const size_t smc = sizeof(int) * ntiles;
+    const int gcount = (int)std::min<int64_t>((n + 4095) / 4096, 4 * nsm);
+    const int gscat = (int)((n + 512 * kScatterItems - 1) / (512 * kScatterItems));
+    k_bin_count<<<gcount, 512, smc, st>>>(smp, counts, ntiles);
+    CUNA_CK(cudaGetLastError());
+    mark(pr, "bin_count", st);
+    static bool attrs = false;
+    if (!attrs) {
+      CUNA_CK(cudaFuncSetAttribute(k_bin_scan_scatter<SampAccS<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(int) * (3 * kScanFuseTiles + 1))));
+      attrs = true;
+    }
+    k_bin_scan_scatter<<<gscat, 512, sizeof(int) * (3 * ntiles + 1), st>>>(sms, counts, offsets, cursor, recs,
+                                                                           ntiles);
+    CUNA_CK(cudaGetLastError());
+    mark(pr, "bin_scatter", st);
+  } else if (n > 0) {
     SampAcc<T> smp{t, y, n, pm, e};
-    const int sms = device_sm_count();
+    const int nsm = device_sm_count();
     const size_t smc = ntiles <= kBinSmemTiles ? sizeof(int) * ntiles : 0;
-    const int gcount = (int)std::min<int64_t>((n + 4095) / 4096, 4 * sms);
+    const int gcount = (int)std::min<int64_t>((n + 4095) / 4096, 4 * nsm);
     const int gscat = (int)((n + 512 * kScatterItems - 1) / (512 * kScatterItems));
     k_bin_count<<<gcount, 512, smc, st>>>(smp, counts, ntiles);
     CUNA_CK(cudaGetLastError());
@@ -257,6 +281,14 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
       attr3 = true;
     }
     k_grid_acc<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+  } else if (p->grid_method == CUNA2_GRID_FIXED) {
+    const size_t smg = grid_fixed_smem_bytes<T>(p->logTL, p->m);
+    static bool attr6 = false;
+    if (!attr6) {
+      CUNA_CK(cudaFuncSetAttribute(k_grid_fixed<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      attr6 = true;
+    }
+    k_grid_fixed<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
   } else {
     const size_t smg = grid_scatter_smem_bytes<T>(p->logTL);
     static bool attr4 = false;
@@ -325,7 +357,11 @@ extern "C" int cuna2_plan_create(cuna2_plan *plan, int dtype, int64_t nf, int R,
   p->m = m;
   p->tau = (double)m * R / (4.0 * kPi * (R - 0.5));
   p->small = logL <= (dtype == CUNA2_F32 ? kSingleLogF32 : kSingleLogF64);
-  p->logTL = ng <= 8192 ? ilog2i(ng) : 12;
+  // default schedule: the fastest measured on GB300 for large grids (float:
+  // 2048-cell gather tiles; double: 4096-cell fixed-point tiles, whose three
+  // exp2 per record spare the FP64 pipe); cuna2_plan_autotune refines it
+  p->logTL = ng <= 8192 ? ilog2i(ng) : (dtype == CUNA2_F32 ? 11 : 12);
+  p->grid_method = dtype == CUNA2_F32 ? CUNA2_GRID_GATHER : CUNA2_GRID_FIXED;
   p->ntiles = (int)(ng >> p->logTL);
   cudaGetDevice(&p->device);
   int st = fft_geometry(dtype == CUNA2_F64, logL, &p->geom);
@@ -485,7 +521,7 @@ namespace cuna {
 namespace {
 bool schedule_ok(const cuna2_plan_st *p, int log_tile, int method) {
   const int logng = ilog2i(p->ng);
-  if (method != CUNA2_GRID_GATHER && method != CUNA2_GRID_SCATTER) return false;
+  if (method < CUNA2_GRID_GATHER || method > CUNA2_GRID_FIXED) return false;
   if (log_tile < 2 || log_tile > logng || log_tile > (method == CUNA2_GRID_GATHER ? 12 : 13)) return false;
   // with more than one tile a record's 2m taps must touch at most two tiles
   return log_tile == logng || (1 << log_tile) >= 2 * p->m;
@@ -557,7 +593,7 @@ extern "C" int cuna2_plan_autotune(cuna2_plan p, const double *t, const void *y,
   if (p->small) {  // one fused CTA per transform: no tiles to choose
     CUNA_TRY(time_schedule(p, t, y, F, n, t0, T, st, reps, &best));
   } else {
-    for (int method = CUNA2_GRID_GATHER; method <= CUNA2_GRID_SCATTER; ++method)
+    for (int method = CUNA2_GRID_GATHER; method <= CUNA2_GRID_FIXED; ++method)
       for (int lt = 9; lt <= 13; ++lt) {
         if (!schedule_ok(p, lt, method) || lt == logng) continue;
         drop_graphs(p);

@@ -54,9 +54,9 @@ __device__ __forceinline__ double frac_of(uint64_t lo, double) {
   return (double)(lo >> 11) * 1.1102230246251565e-16;
 }
 
+// cell and fractional cell of the phase S = frac(x + 1/2) * 2^64
 template <typename T>
-__device__ __forceinline__ void reduce_sample(double t, const PhaseMul &pm, int64_t ng, int &cell, T &f) {
-  const uint64_t S = phase_of(t, pm);
+__device__ __forceinline__ void cell_of_phase(uint64_t S, int64_t ng, int &cell, T &f) {
   if ((ng & (ng - 1)) == 0) {  // ng = 2^g: the top g bits are the cell
     const int g = 63 - __clzll((long long)ng);
     cell = g ? (int)(S >> (64 - g)) : 0;
@@ -65,6 +65,11 @@ __device__ __forceinline__ void reduce_sample(double t, const PhaseMul &pm, int6
     cell = (int)umulhi64(S, (uint64_t)ng);
     f = frac_of(S * (uint64_t)ng, (T)0);
   }
+}
+
+template <typename T>
+__device__ __forceinline__ void reduce_sample(double t, const PhaseMul &pm, int64_t ng, int &cell, T &f) {
+  cell_of_phase<T>(phase_of(t, pm), ng, cell, f);
 }
 
 // ---------------------------------------------------------------------------
@@ -175,6 +180,7 @@ template <typename T> struct SampAcc {
   int64_t n;
   PhaseMul pm;
   AccParams<T> e;
+  uint64_t *sc = nullptr;  // optional: phases written here for SampAccS
   __device__ __forceinline__ Raw load(int64_t i, bool with_value) const {
     Raw r;
     r.t = t[i];
@@ -184,7 +190,43 @@ template <typename T> struct SampAcc {
   __device__ __forceinline__ void prep(int64_t i, const Raw &r, Prep<Rec> &p) const {
     int cell;
     T fr;
-    reduce_sample<T>(r.t, pm, e.ng, cell, fr);
+    const uint64_t S = phase_of(r.t, pm);
+    if (sc) sc[i] = S;
+    cell_of_phase<T>(S, e.ng, cell, fr);
+    const int ng = (int)e.ng;
+    int lo = cell - e.m + 1, hi = cell + e.m;
+    if (lo < 0) lo += ng;
+    if (hi >= ng) hi -= ng;
+    const int t0 = lo >> e.logTL, t1 = hi >> e.logTL;
+    p.t[0] = t0;
+    p.t[1] = t1;
+    p.nt = t0 == t1 ? 1 : 2;
+    rec_set(p.rec, cell, fr, r.y, (int)i);
+  }
+};
+
+// Sampler over phases cached by a SampAcc pass (sc[i] = phase of t[i]): the
+// scatter pass of the binning then skips the phase reduction.
+template <typename T> struct SampAccS {
+  typedef typename RecOf<T>::type Rec;
+  struct Raw {
+    uint64_t S;
+    T y;
+  };
+  const uint64_t *sc;
+  const T *y;
+  int64_t n;
+  AccParams<T> e;
+  __device__ __forceinline__ Raw load(int64_t i, bool with_value) const {
+    Raw r;
+    r.S = sc[i];
+    if (with_value) r.y = y[i];
+    return r;
+  }
+  __device__ __forceinline__ void prep(int64_t i, const Raw &r, Prep<Rec> &p) const {
+    int cell;
+    T fr;
+    cell_of_phase<T>(r.S, e.ng, cell, fr);
     const int ng = (int)e.ng;
     int lo = cell - e.m + 1, hi = cell + e.m;
     if (lo < 0) lo += ng;
@@ -526,6 +568,209 @@ __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 3) k_grid_s
   const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
   grid_tile_scatter<T>(recs, off[tile], off[tile + 1], tile << e.logTL, grid, e, wts, nvals, sbeg, send,
                        slab_stride);
+}
+
+// Fixed-point form: one thread per record, all 2m taps from the fast Gaussian
+// factorisation  y exp2(-k1 (d - f)^2) = [y exp2(-k1 f^2)] Q^d exp2(-k1 d^2),
+// Q = exp2(2 k1 f)  (three exp2 per record, two multiplies per tap), each
+// tap added into the shared tile as an integer with a native shared-memory
+// integer atomic.  The tile's fixed-point scale comes from a bound on every
+// cell's sum: |y| <= Ymax over the tile's records and at most 2 hmax records
+// reach one cell, hmax the largest count of records in a bucket of
+// max(2m, 16) consecutive cells (a cell's 2m-cell window meets two buckets);
+// weights are <= 1.  With the sum bounded by 2^30 (float, int32 cells) or
+// 2^62 (double, int64 cells) units, the quantum is 2^-30 (2^-62) of the
+// bound.  Integer sums do not depend on the order of the atomics, so the grid
+// is bit-reproducible run to run.  A non-finite value makes its tiles NaN.
+template <typename T> struct FixAcc;
+template <> struct FixAcc<float> {
+  typedef int type;
+  static constexpr float range = 1073741824.0f;  // 2^30
+  __device__ static int to_fix(float w) { return __float2int_rn(w); }
+  __device__ static void add(int *a, int v) { atomicAdd(a, v); }
+};
+template <> struct FixAcc<double> {
+  typedef long long type;
+  static constexpr double range = 4611686018427387904.0;  // 2^62
+  __device__ static long long to_fix(double w) { return __double2ll_rn(w); }
+  __device__ static void add(long long *a, long long v) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(a), (unsigned long long)v);
+  }
+};
+
+// exp2 for the gridding weights: ex2.approx for float (relative error of a
+// few ulp), the library exp2 for double
+__device__ __forceinline__ float exp2_g(float x) { return ex2_fast(x); }
+__device__ __forceinline__ double exp2_g(double x) { return exp2(x); }
+
+// records [c0, c0 + cnt) -> srec (values from ws when given); returns the
+// thread's max |value| (NaN once one is not finite)
+template <typename T>
+__device__ __forceinline__ float fixed_stage(const typename RecOf<T>::type *__restrict__ recs, int c0, int cnt,
+                                            int base, const T *__restrict__ ws, SRec<T> *srec) {
+  float ym = 0.f;
+#pragma unroll 1
+  for (int i = threadIdx.x; i < cnt; i += kGridThreads) {
+    const typename RecOf<T>::type rc = recs[c0 + i];
+    SRec<T> r;
+    r.f = rc.a;
+    r.y = ws ? ws[rc.p] : rc.b;
+    r.lc = rc.cell - base;
+    r.pad = rc.p;
+    srec[i] = r;
+    ym = isfinite(r.y) && !isnan(ym) ? fmaxf(ym, (float)fabs(r.y)) : __int_as_float(0x7fffffff);
+  }
+  return ym;
+}
+
+template <typename T>
+__device__ __forceinline__ void grid_tile_fixed(const typename RecOf<T>::type *__restrict__ recs, int r0, int r1,
+                                                int base, T *__restrict__ grid, const AccParams<T> &e,
+                                                const T *__restrict__ wts, int64_t nvals, int sbeg, int send,
+                                                int64_t slab_stride) {
+  typedef FixAcc<T> FA;
+  typedef typename FA::type A;
+  constexpr int CAP = GridCfg<T>::CAP;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ float red[kGridThreads / 32];
+  __shared__ int redi[kGridThreads / 32];
+  __shared__ T scale_s;
+  const int TL = 1 << e.logTL, m = e.m;
+  const int gmask = (int)e.ng - 1;
+  int logBS = 4;
+  while ((1 << logBS) < 2 * m) ++logBS;
+  const int NB = ((TL + 2 * m) >> logBS) + 1;
+  A *acc = reinterpret_cast<A *>(smem_raw);                                  // TL cells
+  SRec<T> *srec = reinterpret_cast<SRec<T> *>(smem_raw + sizeof(A) * TL);    // CAP staged records
+  T *cd = reinterpret_cast<T *>(srec + CAP);                                 // exp2(-k1 d^2), d = -m+1..m
+  int *hist = reinterpret_cast<int *>(cd + 32);                              // NB buckets
+  const int nchunks = (r1 - r0 + CAP - 1) / CAP;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int d = threadIdx.x; d < 2 * m; d += kGridThreads) {
+    const T dd = (T)(d - m + 1);
+    cd[d] = exp2_g(-e.k1 * dd * dd);
+  }
+  // bucket histogram of the tile's records (slab independent); a record of
+  // this tile lies in [base - m, base + TL + m) modulo ng
+  for (int b = threadIdx.x; b < NB; b += kGridThreads) hist[b] = 0;
+  __syncthreads();
+#pragma unroll 1
+  for (int i = r0 + threadIdx.x; i < r1; i += kGridThreads)
+    atomicAdd(&hist[((recs[i].cell - base + m) & gmask) >> logBS], 1);
+  __syncthreads();
+  int hmax = 0;
+  for (int b = threadIdx.x; b < NB; b += kGridThreads) hmax = max(hmax, hist[b]);
+  for (int o = 16; o > 0; o >>= 1) hmax = max(hmax, __shfl_xor_sync(0xffffffffu, hmax, o));
+  if (lane == 0) redi[warp] = hmax;
+  __syncthreads();
+  hmax = 0;
+#pragma unroll
+  for (int w = 0; w < kGridThreads / 32; ++w) hmax = max(hmax, redi[w]);
+  for (int slab = sbeg; slab < send; ++slab) {
+    const T *ws = wts ? wts + (int64_t)slab * nvals : nullptr;
+    float ym = 0.f;
+    if (slab > sbeg) __syncthreads();  // the previous slab's flush is done with acc and srec
+    if (nchunks == 1) {
+      ym = fixed_stage<T>(recs, r0, r1 - r0, base, ws, srec);
+    } else {  // bound pass over all of the tile's records
+#pragma unroll 1
+      for (int i = r0 + threadIdx.x; i < r1; i += kGridThreads) {
+        const T v = ws ? ws[recs[i].p] : recs[i].b;
+        ym = isfinite(v) && !isnan(ym) ? fmaxf(ym, (float)fabs(v)) : __int_as_float(0x7fffffff);
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const float u = __shfl_xor_sync(0xffffffffu, ym, o);
+      ym = (isnan(u) || isnan(ym)) ? __int_as_float(0x7fffffff) : fmaxf(ym, u);
+    }
+    if (lane == 0) red[warp] = ym;
+    for (int i = threadIdx.x; i < TL; i += kGridThreads) acc[i] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float y = 0.f;
+      bool bad = false;
+      for (int w = 0; w < kGridThreads / 32; ++w) {
+        bad |= isnan(red[w]);
+        y = fmaxf(y, red[w]);
+      }
+      // bound on any cell's |sum| in value units; the scale maps it to `range`
+      const T B = (T)y * (T)(2 * hmax);
+      T sc = B > (T)0 ? FA::range / B : (T)0;
+      if (isinf(sc)) sc = (T)0;
+      scale_s = bad ? (T)NAN : sc;
+    }
+    __syncthreads();
+    const T sc = scale_s;
+    for (int ck = 0; ck < nchunks; ++ck) {
+      const int c0 = r0 + ck * CAP;
+      const int cnt = min(CAP, r1 - c0);
+      if (nchunks > 1) {
+        if (ck > 0) __syncthreads();
+        fixed_stage<T>(recs, c0, cnt, base, ws, srec);
+        __syncthreads();
+      }
+      if (sc > (T)0) {
+#pragma unroll 1
+        for (int i = threadIdx.x; i < cnt; i += kGridThreads) {
+          const SRec<T> q = srec[i];
+          const T E = q.y * sc * exp2_g(-e.k1 * q.f * q.f);
+          const T Q = exp2_g(e.k2 * q.f), Qi = exp2_g(-e.k2 * q.f);
+          const int p0 = q.lc;
+          if (p0 - m + 1 >= 0 && p0 + m < TL) {  // every tap inside the tile
+            A *a = acc + p0;
+            T u = E;
+#pragma unroll 4
+            for (int d = 0; d <= m; ++d) {  // taps right of the cell, Q^d
+              FA::add(a + d, FA::to_fix(u * cd[d + m - 1]));
+              u *= Q;
+            }
+            u = E * Qi;
+#pragma unroll 4
+            for (int d = -1; d > -m; --d) {  // taps left of the cell
+              FA::add(a + d, FA::to_fix(u * cd[d + m - 1]));
+              u *= Qi;
+            }
+          } else {  // near the tile edge: wrap, keep the taps inside the tile
+            T u = E;
+            for (int d = 0; d <= m; ++d) {
+              const int lc = (p0 + d) & gmask;
+              if (lc < TL) FA::add(&acc[lc], FA::to_fix(u * cd[d + m - 1]));
+              u *= Q;
+            }
+            u = E * Qi;
+            for (int d = -1; d > -m; --d) {
+              const int lc = (p0 + d) & gmask;
+              if (lc < TL) FA::add(&acc[lc], FA::to_fix(u * cd[d + m - 1]));
+              u *= Qi;
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // fixed-order flush: cell = integer / scale
+    T *out = grid + (int64_t)slab * slab_stride + base;
+    const T inv = sc > (T)0 ? (T)1 / sc : (sc == sc ? (T)0 : sc);
+    for (int i = 4 * threadIdx.x; i < TL; i += 4 * kGridThreads)
+      store4(out + i, (T)acc[i] * inv, (T)acc[i + 1] * inv, (T)acc[i + 2] * inv, (T)acc[i + 3] * inv);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 2) k_grid_fixed(
+    const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
+    AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab, int group, int64_t slab_stride) {
+  const int tile = blockIdx.x;
+  const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
+  grid_tile_fixed<T>(recs, off[tile], off[tile + 1], tile << e.logTL, grid, e, wts, nvals, sbeg, send, slab_stride);
+}
+
+template <typename T> size_t grid_fixed_smem_bytes(int logTL, int m) {
+  int logBS = 4;
+  while ((1 << logBS) < 2 * m) ++logBS;
+  const size_t NB = ((((size_t)1 << logTL) + 2 * m) >> logBS) + 1;
+  return sizeof(typename FixAcc<T>::type) * ((size_t)1 << logTL) + sizeof(SRec<T>) * (size_t)GridCfg<T>::CAP +
+         sizeof(T) * 32 + sizeof(int) * NB;
 }
 
 template <typename T> size_t grid_scatter_smem_bytes(int logTL) {

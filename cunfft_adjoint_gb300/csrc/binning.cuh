@@ -12,6 +12,8 @@
 //   k_scan_tiles  exclusive scan counts -> offsets[0..ntiles], cursor = 0
 //   k_bin_scatter per-CTA shared ranks + one global reservation per
 //                 (CTA, tile) -> records in tile order
+//   k_bin_scan_scatter  the last two in one launch (each CTA scans the
+//                 counts itself) for up to kScanFuseTiles tiles
 //
 // The tile index of a sample is an exact integer function of its input (the
 // bucket indices are bit-exact); only the order of records inside a tile
@@ -157,6 +159,90 @@ __global__ void __launch_bounds__(512) k_bin_scatter(S smp, const int *__restric
       const int pos = sm ? lbase[p[it].t[q]] + rk[it][q] : rk[it][q];
       recs[pos] = p[it].rec;
     }
+}
+
+// Exclusive scan of n ints in shared memory by the whole CTA (blockDim.x a
+// multiple of 32, <= 1024): out[i] = sum_{u<i} in[u], out[n] = total.  `in`
+// and `out` may not alias.  Ends with a barrier.
+__device__ __forceinline__ void cta_exclusive_scan(const int *in, int *out, int n) {
+  __shared__ int wsum[32];
+  const int nt = blockDim.x, tid = threadIdx.x;
+  const int per = (n + nt - 1) / nt;
+  const int beg = min(tid * per, n), end = min(beg + per, n);
+  int sum = 0;
+  for (int i = beg; i < end; ++i) sum += in[i];
+  const int lane = tid & 31, w = tid >> 5;
+  int v = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += u;
+  }
+  if (lane == 31) wsum[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    int s = lane < (nt >> 5) ? wsum[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += u;
+    }
+    wsum[lane] = s;
+  }
+  __syncthreads();
+  int run = v - sum + (w > 0 ? wsum[w - 1] : 0);
+  for (int i = beg; i < end; ++i) {
+    out[i] = run;
+    run += in[i];
+  }
+  if (tid == nt - 1) out[n] = wsum[(nt >> 5) - 1];
+  __syncthreads();
+}
+
+// k_bin_scan_scatter: k_scan_tiles folded into k_bin_scatter.  Every CTA
+// scans the tile counts itself (ntiles <= kScanFuseTiles ints, from L2) and
+// CTA 0 also publishes offsets[0..ntiles] for the gridding.  cursor[] must be
+// zero on entry.
+constexpr int kScanFuseTiles = 4096;  // 3 shared arrays of ntiles ints: 48 KB
+
+template <class S>
+__global__ void __launch_bounds__(512) k_bin_scan_scatter(S smp, const int *__restrict__ counts,
+                                                          int *__restrict__ offsets, int *__restrict__ cursor,
+                                                          typename S::Rec *__restrict__ recs, int ntiles) {
+  typedef typename S::Rec Rec;
+  extern __shared__ int sh[];
+  int *lc = sh, *lbase = sh + ntiles, *off = sh + 2 * ntiles;  // off: ntiles + 1
+  for (int t = threadIdx.x; t < ntiles; t += blockDim.x) {
+    lc[t] = 0;
+    lbase[t] = counts[t];
+  }
+  __syncthreads();
+  cta_exclusive_scan(lbase, off, ntiles);
+  if (blockIdx.x == 0)
+    for (int t = threadIdx.x; t <= ntiles; t += blockDim.x) offsets[t] = off[t];
+  const int64_t chunk0 = (int64_t)blockIdx.x * blockDim.x * kScatterItems;
+  Prep<Rec> p[kScatterItems];
+  int rk[kScatterItems][2];
+  typename S::Raw raw[kScatterItems];
+#pragma unroll
+  for (int it = 0; it < kScatterItems; ++it) {
+    const int64_t i = chunk0 + (int64_t)it * blockDim.x + threadIdx.x;
+    if (i < smp.n) raw[it] = smp.load(i, true);
+  }
+#pragma unroll
+  for (int it = 0; it < kScatterItems; ++it) {
+    const int64_t i = chunk0 + (int64_t)it * blockDim.x + threadIdx.x;
+    p[it].nt = 0;
+    if (i < smp.n) smp.prep(i, raw[it], p[it]);
+    for (int q = 0; q < p[it].nt; ++q) rk[it][q] = atomicAdd(&lc[p[it].t[q]], 1);
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < ntiles; t += blockDim.x)
+    if (lc[t]) lbase[t] = off[t] + atomicAdd(&cursor[t], lc[t]);
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < kScatterItems; ++it)
+    for (int q = 0; q < p[it].nt; ++q) recs[lbase[p[it].t[q]] + rk[it][q]] = p[it].rec;
 }
 
 }  // namespace

@@ -234,12 +234,19 @@ int cuna2_plan_profile(cuna2_plan plan, const double *t, const void *y, void *F,
  *                       shared memory and each thread sums four consecutive
  *                       cells over its window of records (log_tile <= 12);
  *   CUNA2_GRID_SCATTER  one thread per (record, tap) adds its Gaussian weight
- *                       into the shared tile (log_tile <= 13).
- * Both compute the same sums.  With more than one tile, 2^log_tile >= 2m.
- * New plans start at (min(log2 ng, 12), CUNA2_GRID_SCATTER).  Changing the
+ *                       into the shared tile with an atomic (log_tile <= 13);
+ *   CUNA2_GRID_FIXED    one thread per record computes all 2m taps from the
+ *                       factorised Gaussian and adds them as fixed-point
+ *                       integers (int32 cells for float plans, int64 for
+ *                       double) scaled to a per-tile bound on the cell sums,
+ *                       so the grid is bit-reproducible (log_tile <= 13).
+ * All compute the same sums to rounding.  With more than one tile,
+ * 2^log_tile >= 2m.
+ * New plans start at (11, CUNA2_GRID_GATHER) for float and (12,
+ * CUNA2_GRID_FIXED) for double (a grid of at most 8192 cells is one tile).  Changing the
  * schedule drops the plan's cached graphs.  No counterpart in the reference
  * (its gridding kernel, src/gridding.cu:36-65, has a fixed launch shape). */
-enum { CUNA2_GRID_GATHER = 0, CUNA2_GRID_SCATTER = 1 };
+enum { CUNA2_GRID_GATHER = 0, CUNA2_GRID_SCATTER = 1, CUNA2_GRID_FIXED = 2 };
 int cuna2_plan_set_schedule(cuna2_plan plan, int log_tile, int grid_method);
 int cuna2_plan_get_schedule(cuna2_plan plan, int *log_tile, int *grid_method);
 

@@ -135,8 +135,8 @@ SCHED_CASES = [
 
 @pytest.mark.parametrize("n,nf,R,m,dtype,tol", SCHED_CASES)
 def test_every_schedule(nfft, oracle_lib, n, nf, R, m, dtype, tol):
-    """Both gridding forms at every admissible tile size give the NDFT's
-    spectrum; the two forms agree with each other to rounding."""
+    """Every gridding form at every admissible tile size gives the NDFT's
+    spectrum; the forms agree with each other to rounding."""
     from cunfft_adjoint_gb300 import _lib
     rng = np.random.default_rng(n)
     t = rng.uniform(0, 500.0, n)
@@ -148,7 +148,7 @@ def test_every_schedule(nfft, oracle_lib, n, nf, R, m, dtype, tol):
     sel = np.sort(rng.choice(k, 256, replace=False))
     D = oracle_lib.ndft(t, y.astype(np.float64), 0.0, 500.0, sel)
     outs = {}
-    for gm in (_lib.GRID_GATHER, _lib.GRID_SCATTER):
+    for gm in (_lib.GRID_GATHER, _lib.GRID_SCATTER, _lib.GRID_FIXED):
         for lt in (9, 10, 11, 12, 13):
             if gm == _lib.GRID_GATHER and lt == 13:
                 with pytest.raises(_lib.CunaError):
@@ -170,7 +170,7 @@ def test_schedule_rejects_bad_values(nfft):
     for lt, gm in ((4, _lib.GRID_SCATTER), (14, _lib.GRID_SCATTER), (12, 7), (1, _lib.GRID_GATHER)):
         with pytest.raises(_lib.CunaError):
             plan.set_schedule(lt, gm)
-    assert plan.schedule == (12, _lib.GRID_SCATTER)
+    assert plan.schedule == (11, _lib.GRID_GATHER)
 
 
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
@@ -187,14 +187,15 @@ def test_schedules_with_slab_weights(nfft, oracle_lib, dtype):
     Y = torch.stack([yd, yd * 0 + 1, yd * yd])
     plan = nfft.AdjointNFFT(nf, R, m, dtype)
     res = []
-    for gm in (_lib.GRID_GATHER, _lib.GRID_SCATTER):
+    for gm in (_lib.GRID_GATHER, _lib.GRID_SCATTER, _lib.GRID_FIXED):
         plan.set_schedule(11, gm)
         B = plan.bootstrap(td, yd, 40, 17, 0.0, 100.0).cpu().numpy()
         M = plan.multi(td, Y, 0.0, 100.0).cpu().numpy()
         res.append((B, M))
     tol = 2e-6 if dtype == torch.float32 else 1e-13
-    assert rel_l2(res[0][0], res[1][0]) < tol
-    assert rel_l2(res[0][1], res[1][1]) < tol
+    for other in res[1:]:
+        assert rel_l2(res[0][0], other[0]) < tol
+        assert rel_l2(res[0][1], other[1]) < tol
     D = oracle_lib.ndft(t, np.ones(n), 0.0, 100.0, np.arange(-nf // 2, nf // 2)[::64])
     # m = 8, R = 4: Gaussian kernel accuracy about exp(-pi m sqrt(1 - 1/R)) = 3.5e-10
     assert rel_l2(res[1][1][1][::64], D) < (1e-5 if dtype == torch.float32 else 2e-9)
@@ -211,10 +212,31 @@ def test_autotune(nfft, oracle_lib, dtype):
     yd = torch.as_tensor(y, dtype=dtype, device="cuda")
     plan = nfft.AdjointNFFT(nf, 2, 8, dtype)
     lt, gm, ms = plan.autotune(td, yd, 0.0, 1000.0, reps=3)
-    assert 9 <= lt <= 13 and gm in (_lib.GRID_GATHER, _lib.GRID_SCATTER) and ms > 0
+    assert 9 <= lt <= 13 and gm in (_lib.GRID_GATHER, _lib.GRID_SCATTER, _lib.GRID_FIXED)
+    assert ms > 0
     assert plan.schedule == (lt, gm)
     F = plan(td, yd, 0.0, 1000.0).cpu().numpy().astype(np.complex128)
     sel = np.sort(rng.choice(np.arange(-nf // 2, nf // 2), 128, replace=False))
     D = oracle_lib.ndft(t, y, 0.0, 1000.0, sel)
     # m = 8, R = 2: Gaussian kernel accuracy about exp(-pi m sqrt(1 - 1/R)) = 1.9e-8
     assert rel_l2(F[sel + nf // 2], D) < (1e-5 if dtype == torch.float32 else 5e-8)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_fixed_point_grid_is_reproducible(nfft, dtype):
+    """The fixed-point form sums integers, so repeated runs (different atomic
+    orders) give bit-identical spectra; a non-finite value turns its tiles,
+    and so the spectrum, into NaN as float accumulation would."""
+    from cunfft_adjoint_gb300 import _lib
+    rng = np.random.default_rng(21)
+    n, nf = 400_000, 1 << 17
+    t = torch.as_tensor(rng.uniform(0, 100.0, n), device="cuda")
+    y = torch.as_tensor(rng.normal(0, 1, n), dtype=dtype, device="cuda")
+    plan = nfft.AdjointNFFT(nf, 2, 8, dtype)
+    plan.set_schedule(12, _lib.GRID_FIXED)
+    F1 = plan(t, y, 0.0, 100.0).clone()
+    F2 = plan(t, y, 0.0, 100.0).clone()
+    assert torch.equal(F1, F2)
+    y[123] = float("nan")
+    F3 = plan(t, y, 0.0, 100.0)
+    assert torch.isnan(F3.real).any()
