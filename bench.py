@@ -329,6 +329,8 @@ def main():
     ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-side-legs", action="store_true", help="skip the float64 and batched legs")
     ap.add_argument("--nsets", type=int, default=NSETS, help="rotating input sets (default 16: 192 MB > L2)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
@@ -351,6 +353,8 @@ def main():
     Fd = [torch.empty(nf, dtype=torch.complex64, device=dev) for _ in range(4)]
     plan = AdjointNFFT(nf, R, m, torch.float32, device=dev)
     L = _lib.core()
+    # the plan's own autotuner picks the tile size and gridding form on input set 0
+    schedule = plan.autotune(td[0], yd[0], 0.0, T, reps=5)[:2] if not args.no_autotune else plan.schedule
     if not args.no_graph:
         _lib.check(L.cuna2_plan_set_graph(plan._h, 1))
     stream = torch.cuda.current_stream(dev)
@@ -432,11 +436,13 @@ def main():
 
     # float64 side by side (same workload, double plan)
     f64 = None
-    if rank == 0:
+    if rank == 0 and not args.no_side_legs:
         plan64 = AdjointNFFT(nf, R, m, torch.float64, device=dev)
+        yd64 = [torch.as_tensor(y, dtype=torch.float64, device=dev) for y in ys[:4]]
+        if not args.no_autotune:
+            plan64.autotune(td[0], yd64[0], 0.0, T, reps=2)
         if not args.no_graph:
             _lib.check(L.cuna2_plan_set_graph(plan64._h, 1))
-        yd64 = [torch.as_tensor(y, dtype=torch.float64, device=dev) for y in ys[:4]]
         n64 = len(yd64)
         F64 = torch.empty(nf, dtype=torch.complex128, device=dev)
         for s in range(8):
@@ -454,7 +460,7 @@ def main():
         f64 = {"value": 1000.0 / ms64, "unit": UNIT, "ms_per_step": ms64, "rel_err_vs_fp64_ndft": err64,
                "steps": k64}
 
-    batched = batched_legs(dev, args.steps) if rank == 0 else None
+    batched = batched_legs(dev, args.steps) if rank == 0 and not args.no_side_legs else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -469,7 +475,9 @@ def main():
                        "mode": "accurate (fixed-point phase, float32 gridding+FFT)",
                        "cache": "%d rotating input sets (%.0f MB of t,y; L2 is 129 MB)" %
                                 (nsets, nsets * n * 12 / 1e6),
-                       "graph": not args.no_graph, "parallelism": "replicas" if ws > 1 else "single"},
+                       "graph": not args.no_graph, "parallelism": "replicas" if ws > 1 else "single",
+                       "schedule": {"log_tile": schedule[0],
+                                    "grid_method": ["gather", "scatter", "fixed"][schedule[1]]}},
             "rel_err_vs_fp64_ndft": err,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
