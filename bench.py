@@ -145,6 +145,7 @@ def stage_bytes(n, ng, nf, rec_bytes=16, elem=4):
     L = ng // 2
     c = 2 * elem
     return {
+        "bin_local": 8 * n + elem * n + rec_bytes * n,       # read t, y; write records (chunk-local order)
         "bin_count": 16 * n,                                 # read t; write the 64-bit phases
         "scan_tiles": 0,
         "bin_scatter": 8 * n + elem * n + rec_bytes * n,     # read phases, y; write records

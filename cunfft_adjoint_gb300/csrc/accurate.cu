@@ -186,11 +186,29 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   const FftDev<T> f = to_dev<T>(p->geom);
   const int L = 1 << p->geom.logL;
   const int ntiles = p->ntiles;
-  // workspace: counts | cursor | offsets | phases | records | grid slabs | weights
+  // binning: single pass into chunk-local tile order (k_bin_local) when the
+  // chunk table stays small, else count + scan/scatter into one global order.
+  // Chunks of CH samples: at least two per SM, at most kSegMaxChunks.
+  const int nsm = device_sm_count();
+  int CH = 0, nch = 0;
+  if (!p->small && n > 0 && ntiles <= kScanFuseTiles) {
+    int64_t want = std::max<int64_t>(std::max<int64_t>((n + 2 * nsm - 1) / (2 * nsm),
+                                                       (n + kSegMaxChunks - 1) / kSegMaxChunks), 1024);
+    want = (want + 511) / 512 * 512;
+    if (want <= 16384) {
+      CH = (int)want;
+      nch = (int)((n + CH - 1) / CH);
+    }
+  }
+  const bool seg = nch > 0;
+  // workspace: counts | cursor | offsets | phases or chunk table | records | grid slabs | weights
   const size_t o_cnt = 0, o_cur = align_up(sizeof(int) * ntiles), o_off = 2 * o_cur;
   const size_t o_phs = o_off + align_up(sizeof(int) * (ntiles + 1));
-  const size_t o_rec = o_phs + (p->small ? 0 : align_up(sizeof(uint64_t) * (size_t)(n > 0 ? n : 1)));
-  const size_t o_grid = o_rec + (p->small ? 0 : align_up(sizeof(Rec) * 2 * (size_t)(n > 0 ? n : 1)));
+  const size_t nrec = seg ? 2 * ((size_t)n + CH) : 2 * (size_t)(n > 0 ? n : 1);
+  const size_t o_rec = o_phs + (p->small ? 0
+                                         : (seg ? align_up(sizeof(int) * (size_t)ntiles * nch)
+                                                : align_up(sizeof(uint64_t) * (size_t)(n > 0 ? n : 1))));
+  const size_t o_grid = o_rec + (p->small ? 0 : align_up(sizeof(Rec) * nrec));
   const size_t o_wts = o_grid + (p->small ? 0 : align_up(sizeof(T) * (size_t)p->ng * nslab));
   const size_t bytes = o_wts + (nbs > 0 ? sizeof(T) * (size_t)n * nbs : 0) + 256;
   void *ws = nullptr;
@@ -198,6 +216,7 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   char *w = (char *)ws;
   int *counts = (int *)(w + o_cnt), *offsets = (int *)(w + o_off), *cursor = (int *)(w + o_cur);
   uint64_t *phases = (uint64_t *)(w + o_phs);
+  int *loc = (int *)(w + o_phs);  // chunk table of the single-pass binning
   Rec *recs = (Rec *)(w + o_rec);
   T *grid = (T *)(w + o_grid);
   T *wts = multi ? const_cast<T *>(multi) : (nbs > 0 ? (T *)(w + o_wts) : nullptr);
@@ -228,13 +247,18 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     mark(pr, "nfft_small", st);
     return CUNA2_SUCCESS;
   }
+  if (seg) {
+    SampAcc<T> smp{t, y, n, pm, e};
+    k_bin_local<<<nch, 512, sizeof(int) * (2 * ntiles + 1), st>>>(smp, recs, loc, ntiles, nch, CH);
+    CUNA_CK(cudaGetLastError());
+    mark(pr, "bin_local", st);
+  } else {
   // counts and cursor are adjacent: one memset zeroes both
   CUNA_CK(cudaMemsetAsync(counts, 0, o_off, st));
   if (n > 0 && ntiles <= kScanFuseTiles) {
     // count (caching each sample's phase), then scan + scatter in one launch
     SampAcc<T> smp{t, y, n, pm, e, phases};
     SampAccS<T> sms{phases, y, n, e};
-    const int nsm = device_sm_count();
     const size_t smc = sizeof(int) * ntiles;
     const int gcount = (int)std::min<int64_t>((n + 4095) / 4096, 4 * nsm);
     const int gscat = (int)((n + 512 * kScatterItems - 1) / (512 * kScatterItems));
@@ -253,7 +277,6 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     mark(pr, "bin_scatter", st);
   } else if (n > 0) {
     SampAcc<T> smp{t, y, n, pm, e};
-    const int nsm = device_sm_count();
     const size_t smc = ntiles <= kBinSmemTiles ? sizeof(int) * ntiles : 0;
     const int gcount = (int)std::min<int64_t>((n + 4095) / 4096, 4 * nsm);
     const int gscat = (int)((n + 512 * kScatterItems - 1) / (512 * kScatterItems));
@@ -270,33 +293,46 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     k_scan_tiles<<<1, 1024, 0, st>>>(counts, offsets, cursor, ntiles);
     CUNA_CK(cudaGetLastError());
   }
+  }
   // bootstrap / channels: each CTA grids a group of slabs of one tile, reusing its staged records
   const int group = wts ? std::min(8, nslab) : 1;
   const dim3 ggrid(ntiles, (nslab + group - 1) / group);
-  if (p->grid_method == CUNA2_GRID_GATHER) {
-    const size_t smg = grid_smem_bytes<T>(p->logTL, p->m);
-    static bool attr3 = false;
-    if (!attr3) {
-      CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-      attr3 = true;
-    }
-    k_grid_acc<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
-  } else if (p->grid_method == CUNA2_GRID_FIXED) {
-    const size_t smg = grid_fixed_smem_bytes<T>(p->logTL, p->m);
-    static bool attr6 = false;
-    if (!attr6) {
-      CUNA_CK(cudaFuncSetAttribute(k_grid_fixed<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-      attr6 = true;
-    }
-    k_grid_fixed<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+  // the chunk runs of a tile sit behind the form's own shared memory
+  const size_t segb = seg ? sizeof(int) * (2 * (size_t)nch + 1) : 0;
+  const int ch2 = 2 * CH;
+  static bool attr_done = false;
+  if (!attr_done) {
+    const int mx = 200 * 1024;
+    CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_fixed<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_acc_seg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_fixed_seg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_scatter_seg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    attr_done = true;
+  }
+  size_t smg;
+  if (p->grid_method == CUNA2_GRID_GATHER) smg = grid_smem_bytes<T>(p->logTL, p->m);
+  else if (p->grid_method == CUNA2_GRID_FIXED) smg = grid_fixed_smem_bytes<T>(p->logTL, p->m);
+  else smg = grid_scatter_smem_bytes<T>(p->logTL);
+  smg = (smg + 15) & ~(size_t)15;
+  if (seg) {
+    if (p->grid_method == CUNA2_GRID_GATHER)
+      k_grid_acc_seg<T><<<ggrid, kGridThreads, smg + segb, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n,
+                                                                  nslab, group, p->ng);
+    else if (p->grid_method == CUNA2_GRID_FIXED)
+      k_grid_fixed_seg<T><<<ggrid, kGridThreads, smg + segb, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n,
+                                                                    nslab, group, p->ng);
+    else
+      k_grid_scatter_seg<T><<<ggrid, kGridThreads, smg + segb, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts,
+                                                                      n, nslab, group, p->ng);
   } else {
-    const size_t smg = grid_scatter_smem_bytes<T>(p->logTL);
-    static bool attr4 = false;
-    if (!attr4) {
-      CUNA_CK(cudaFuncSetAttribute(k_grid_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-      attr4 = true;
-    }
-    k_grid_scatter<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+    if (p->grid_method == CUNA2_GRID_GATHER)
+      k_grid_acc<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+    else if (p->grid_method == CUNA2_GRID_FIXED)
+      k_grid_fixed<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+    else
+      k_grid_scatter<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
   }
   CUNA_CK(cudaGetLastError());
   mark(pr, "grid", st);

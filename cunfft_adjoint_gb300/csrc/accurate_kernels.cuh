@@ -49,7 +49,11 @@ template <typename T> struct AccParams {
 };
 
 // fractional cell from the low word of S*ng
-__device__ __forceinline__ float frac_of(uint64_t lo, float) { return (float)(lo >> 40) * 5.9604644775390625e-08f; }
+// (the float version converts a 32-bit integer: 64-bit integer to float
+// conversions run on the narrow FP64 pipe of GB300)
+__device__ __forceinline__ float frac_of(uint64_t lo, float) {
+  return (float)(uint32_t)(lo >> 40) * 5.9604644775390625e-08f;
+}
 __device__ __forceinline__ double frac_of(uint64_t lo, double) {
   return (double)(lo >> 11) * 1.1102230246251565e-16;
 }
@@ -82,9 +86,9 @@ __device__ __forceinline__ void acc_output(const AccParams<T> &e, int64_t k, typ
   const C A = cadd(Zk, Zmc);
   const C Bv = cmuli(csub(Zmc, Zk));
   T sn, cs;
-  sincospi_t((T)k * e.twk, &sn, &cs);
+  const T kf = (T)(int)k;  // k <= nf/2 < 2^31; a 32-bit conversion
+  sincospi_t(kf * e.twk, &sn, &cs);
   const C G2 = cadd(A, cmul(cmk(cs, sn), Bv));
-  const T kf = (T)k;
   T sc = e.c0 * exp_t(e.c1 * kf * kf);
   if (k & 1) sc = -sc;
   const C Fk = cscale(G2, sc);
@@ -326,8 +330,8 @@ __device__ __forceinline__ void grid_slots(int p0, int ng, int TL, int m, int &s
 // One grid tile [base, base + 2^logTL) from records [r0, r1), for slabs
 // [sbeg, send): slab s grids value wts[s*nvals + p] of sample p when wts is
 // given (bootstrap), else the record's own value.
-template <typename T>
-__device__ __forceinline__ void grid_tile_body(const typename RecOf<T>::type *__restrict__ recs, int r0, int r1,
+template <typename T, class Src>
+__device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
                                                int base, T *__restrict__ grid, const AccParams<T> &e,
                                                const T *__restrict__ wts, int64_t nvals, int sbeg, int send,
                                                int64_t slab_stride) {
@@ -501,8 +505,8 @@ __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 4 : 2) k_grid_a
 // every lane of a warp does useful work whatever the record density.  A tap
 // lands in cell (cell + d) mod ng, kept when it falls in this tile; ng is a
 // power of two.  Summation order within a cell follows the atomics.
-template <typename T>
-__device__ __forceinline__ void grid_tile_scatter(const typename RecOf<T>::type *__restrict__ recs, int r0, int r1,
+template <typename T, class Src>
+__device__ __forceinline__ void grid_tile_scatter(const Src &recs, int r0, int r1,
                                                   int base, T *__restrict__ grid, const AccParams<T> &e,
                                                   const T *__restrict__ wts, int64_t nvals, int sbeg, int send,
                                                   int64_t slab_stride) {
@@ -605,8 +609,8 @@ __device__ __forceinline__ double exp2_g(double x) { return exp2(x); }
 
 // records [c0, c0 + cnt) -> srec (values from ws when given); returns the
 // thread's max |value| (NaN once one is not finite)
-template <typename T>
-__device__ __forceinline__ float fixed_stage(const typename RecOf<T>::type *__restrict__ recs, int c0, int cnt,
+template <typename T, class Src>
+__device__ __forceinline__ float fixed_stage(const Src &recs, int c0, int cnt,
                                             int base, const T *__restrict__ ws, SRec<T> *srec) {
   float ym = 0.f;
 #pragma unroll 1
@@ -623,8 +627,8 @@ __device__ __forceinline__ float fixed_stage(const typename RecOf<T>::type *__re
   return ym;
 }
 
-template <typename T>
-__device__ __forceinline__ void grid_tile_fixed(const typename RecOf<T>::type *__restrict__ recs, int r0, int r1,
+template <typename T, class Src>
+__device__ __forceinline__ void grid_tile_fixed(const Src &recs, int r0, int r1,
                                                 int base, T *__restrict__ grid, const AccParams<T> &e,
                                                 const T *__restrict__ wts, int64_t nvals, int sbeg, int send,
                                                 int64_t slab_stride) {
@@ -773,6 +777,63 @@ template <typename T> size_t grid_fixed_smem_bytes(int logTL, int m) {
          sizeof(T) * 32 + sizeof(int) * NB;
 }
 
+// ---------------------------------------------------------------------------
+// Tiles fed by the single-pass chunk-local binning (k_bin_local): a tile's
+// records are nch runs, one per input chunk, located by loc[tile nch + c] =
+// start | count << 16 within chunk c's region recs[c ch2 ..].
+// ---------------------------------------------------------------------------
+constexpr int kSegMaxChunks = 1024;
+
+// element v of a tile's record list: binary search over the runs
+template <typename T> struct SegSrc {
+  typedef typename RecOf<T>::type Rec;
+  const Rec *recs;
+  const int *pre;   // shared, nch + 1: run c holds list elements [pre[c], pre[c+1])
+  const int *base;  // shared, nch: record index of run c's first element
+  int nch;
+  __device__ __forceinline__ Rec operator[](int v) const {
+    int lo = 0, hi = nch - 1;
+    while (lo < hi) {  // last run with pre <= v (a non-empty one)
+      const int mid = (lo + hi + 1) >> 1;
+      if (pre[mid] <= v) lo = mid;
+      else hi = mid - 1;
+    }
+    return recs[base[lo] + (v - pre[lo])];
+  }
+};
+
+// CTA-wide: the runs of `tile` into shared memory sh (2 nch + 1 ints);
+// returns the length of the tile's record list.  Ends with a barrier.
+__device__ __forceinline__ int seg_setup(const int *__restrict__ loc, int tile, int nch, int ch2, int *sh) {
+  int *pre = sh, *cnt = sh + nch + 1;
+  const int *row = loc + (int64_t)tile * nch;
+  for (int c = threadIdx.x; c < nch; c += blockDim.x) cnt[c] = (unsigned)row[c] >> 16;
+  __syncthreads();
+  cta_exclusive_scan(cnt, pre, nch);
+  for (int c = threadIdx.x; c < nch; c += blockDim.x) cnt[c] = c * ch2 + (row[c] & 0xffff);  // now the run bases
+  __syncthreads();
+  return pre[nch];
+}
+
+#define CUNA_SEG_KERNEL(NAME, BODY, OCC32, OCC64)                                                              \
+  template <typename T>                                                                                       \
+  __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? OCC32 : OCC64) NAME(                        \
+      const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ loc, int nch, int ch2,          \
+      int seg_off, T *__restrict__ grid, AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab,    \
+      int group, int64_t slab_stride) {                                                                         \
+    extern __shared__ __align__(16) unsigned char smem_raw[];                                                   \
+    int *sh = reinterpret_cast<int *>(smem_raw + seg_off);                                                      \
+    const int tile = blockIdx.x;                                                                                \
+    const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);                                       \
+    const int total = seg_setup(loc, tile, nch, ch2, sh);                                                       \
+    const SegSrc<T> src{recs, sh, sh + nch + 1, nch};                                                           \
+    BODY<T>(src, 0, total, tile << e.logTL, grid, e, wts, nvals, sbeg, send, slab_stride);                       \
+  }
+CUNA_SEG_KERNEL(k_grid_acc_seg, grid_tile_body, 4, 2)
+CUNA_SEG_KERNEL(k_grid_scatter_seg, grid_tile_scatter, 6, 3)
+CUNA_SEG_KERNEL(k_grid_fixed_seg, grid_tile_fixed, 6, 2)
+#undef CUNA_SEG_KERNEL
+
 template <typename T> size_t grid_scatter_smem_bytes(int logTL) {
   return sizeof(T) * ((size_t)1 << logTL) + (sizeof(SRec<T>) + sizeof(int)) * (size_t)GridCfg<T>::CAP;
 }
@@ -861,7 +922,7 @@ template <typename T> struct BwdSpec {
     if (k < 0) k += ng;
     if (k >= ng - K) k -= ng;  // to [-K, ng - K)
     if (k >= K || k < -K) return cmk((T)0, (T)0);
-    const T kf = (T)k;
+    const T kf = (T)(int)k;
     T sc = c0b * exp_t(c1 * kf * kf);
     if (k & 1) sc = -sc;
     return cscale(G[k + K], sc);

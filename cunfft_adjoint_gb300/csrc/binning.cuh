@@ -14,6 +14,7 @@
 //                 (CTA, tile) -> records in tile order
 //   k_bin_scan_scatter  the last two in one launch (each CTA scans the
 //                 counts itself) for up to kScanFuseTiles tiles
+//   k_bin_local   one pass, records in chunk-local tile order (see there)
 //
 // The tile index of a sample is an exact integer function of its input (the
 // bucket indices are bit-exact); only the order of records inside a tile
@@ -243,6 +244,42 @@ __global__ void __launch_bounds__(512) k_bin_scan_scatter(S smp, const int *__re
 #pragma unroll
   for (int it = 0; it < kScatterItems; ++it)
     for (int q = 0; q < p[it].nt; ++q) recs[lbase[p[it].t[q]] + rk[it][q]] = p[it].rec;
+}
+
+// k_bin_local: single-pass binning into chunk-local tile order.  CTA c takes
+// the samples [c CH, (c+1) CH), counts its records per tile in shared memory,
+// scans the counts, and writes its records tile by tile into its own region
+// recs[c 2CH ..] (a sample makes at most two records).  loc[tau nch + c] =
+// start | count << 16 describes chunk c's run of tile tau, so the gridding CTA
+// of tau finds its records as nch runs (SegSrc).  No global atomics and no
+// separate count pass: each sample's phase is computed twice (count, write),
+// the second time from an L2-resident t.  Needs 2 CH < 2^16, ntiles <=
+// kScanFuseTiles.
+template <class S>
+__global__ void __launch_bounds__(512) k_bin_local(S smp, typename S::Rec *__restrict__ recs,
+                                                   int *__restrict__ loc, int ntiles, int nch, int CH) {
+  typedef typename S::Rec Rec;
+  extern __shared__ int sh[];
+  int *hist = sh, *cur = sh + ntiles;  // cur: ntiles + 1
+  const int c = blockIdx.x;
+  const int64_t i0 = (int64_t)c * CH, i1 = min(i0 + (int64_t)CH, smp.n);
+  for (int t = threadIdx.x; t < ntiles; t += blockDim.x) hist[t] = 0;
+  __syncthreads();
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    Prep<Rec> p;
+    smp.prep(i, smp.load(i, false), p);
+    for (int q = 0; q < p.nt; ++q) atomicAdd(&hist[p.t[q]], 1);
+  }
+  __syncthreads();
+  cta_exclusive_scan(hist, cur, ntiles);
+  for (int t = threadIdx.x; t < ntiles; t += blockDim.x) loc[(int64_t)t * nch + c] = cur[t] | (hist[t] << 16);
+  __syncthreads();
+  Rec *out = recs + (int64_t)c * 2 * CH;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    Prep<Rec> p;
+    smp.prep(i, smp.load(i, true), p);
+    for (int q = 0; q < p.nt; ++q) out[atomicAdd(&cur[p.t[q]], 1)] = p.rec;
+  }
 }
 
 }  // namespace
