@@ -283,6 +283,22 @@ def dist_setup(backend):
     return ws, rank, local
 
 
+def max_over_ranks(ms, ws, device=None):
+    """The slowest rank's time (the contract's max over ranks); ws == 1: ms."""
+    if ws <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ms, steps, ws):
+    """Whole-job NFFT/s: every rank runs `steps` transforms in the max time."""
+    return ws * steps / (ms / 1000.0)
+
+
 def reference_arm(args, wl):
     ws, rank, local = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
     if rank != 0:
@@ -379,14 +395,11 @@ def main():
             step(s)
         e1.record(stream)
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(e0.elapsed_time(e1), ws, dev)
     if ws > 1:
-        tmax = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tmax.item())
         torch.distributed.barrier()
     ms_step = ms / args.steps
-    value = ws * args.steps / (ms / 1000.0)
+    value = replica_value(ms, args.steps, ws)
 
     # per-launch durations (CUDA events between launches on the plan's stream)
     import ctypes
