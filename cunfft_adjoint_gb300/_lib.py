@@ -20,6 +20,7 @@ STATUS = {0: "CUNA2_SUCCESS", 1: "CUNA2_ERROR_INVALID_VALUE", 2: "CUNA2_ERROR_CU
           3: "CUNA2_ERROR_UNSUPPORTED", 4: "CUNA2_ERROR_ALLOC", 5: "CUNA2_ERROR_CUFFT"}
 F32, F64 = 0, 1
 GRID_GATHER, GRID_SCATTER, GRID_FIXED = 0, 1, 2
+BIN_GLOBAL, BIN_LOCAL = 0, 1
 
 
 class CunaError(RuntimeError):
@@ -72,6 +73,8 @@ CORE_SIGNATURES = {
     "cuna2_lomb_scargle": (_I, [_I, _P, _P, _P, _I64, _I64, _D, _D, _I, _I, _P, _P]),
     "cuna2_plan_set_graph": (_I, [_P, _I]),
     "cuna2_plan_set_schedule": (_I, [_P, _I, _I]),
+    "cuna2_plan_set_binning": (_I, [_P, _I]),
+    "cuna2_plan_get_binning": (_I, [_P, _P]),
     "cuna2_plan_get_schedule": (_I, [_P, _P, _P]),
     "cuna2_plan_autotune": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P, _I, _P]),
     "cuna2_plan_profile": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P, _P, _P, _I, _P]),

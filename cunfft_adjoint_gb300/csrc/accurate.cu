@@ -40,6 +40,7 @@ struct cuna2_plan_st {
   double tau;
   int logTL, ntiles;
   int grid_method = CUNA2_GRID_GATHER;  // tile gridding form (cuna2_plan_set_schedule)
+  int binning = CUNA2_BIN_GLOBAL;      // bucket sort form (cuna2_plan_set_binning)
   bool small;  // single-CTA fused path
   cuna::FftGeom geom;
   int device;
@@ -191,7 +192,7 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   // Chunks of CH samples: at least two per SM, at most kSegMaxChunks.
   const int nsm = device_sm_count();
   int CH = 0, nch = 0;
-  if (!p->small && n > 0 && ntiles <= kScanFuseTiles) {
+  if (p->binning == CUNA2_BIN_LOCAL && !p->small && n > 0 && ntiles <= kScanFuseTiles) {
     int64_t want = std::max<int64_t>(std::max<int64_t>((n + 2 * nsm - 1) / (2 * nsm),
                                                        (n + kSegMaxChunks - 1) / kSegMaxChunks), 1024);
     want = (want + 511) / 512 * 512;
@@ -591,15 +592,18 @@ extern "C" int cuna2_plan_get_schedule(cuna2_plan p, int *log_tile, int *grid_me
   return CUNA2_SUCCESS;
 }
 
-// Time `reps` plain runs of the current schedule on `st` (min over runs).
+// Time `reps` plain runs of the current schedule on `st` (min over runs),
+// each after overwriting `flush` (when given) so that the inputs come from
+// HBM as they do in a stream of different series.
 static int time_schedule(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0, double T,
-                         cudaStream_t st, int reps, float *ms) {
+                         cudaStream_t st, int reps, void *flush, size_t flush_bytes, float *ms) {
   cudaEvent_t a, b;
   CUNA_CK(cudaEventCreate(&a));
   CUNA_CK(cudaEventCreate(&b));
   int s = run_any(p, t, y, F, n, t0, T, st, nullptr);  // warm-up; grows the workspace
   float best = 3.4e38f;
   for (int r = 0; !s && r < reps; ++r) {
+    if (flush) cudaMemsetAsync(flush, r & 0xff, flush_bytes, st);
     cudaEventRecord(a, st);
     s = run_any(p, t, y, F, n, t0, T, st, nullptr);
     cudaEventRecord(b, st);
@@ -624,32 +628,70 @@ extern "C" int cuna2_plan_autotune(cuna2_plan p, const double *t, const void *y,
   if (reps < 1) reps = 5;
   std::lock_guard<std::mutex> lk(p->mu);
   const int logng = ilog2i(p->ng);
-  int best_tile = p->logTL, best_method = p->grid_method;
+  int best_tile = p->logTL, best_method = p->grid_method, best_bin = p->binning;
   float best = 3.4e38f;
+  // a buffer of twice the L2 size, overwritten before each timed run
+  int dev = 0, l2 = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+  void *flush = nullptr;
+  const size_t flush_bytes = 2 * (size_t)(l2 > 0 ? l2 : 0);
+  if (flush_bytes && cudaMalloc(&flush, flush_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    flush = nullptr;
+  }
+  int s = CUNA2_SUCCESS;
   if (p->small) {  // one fused CTA per transform: no tiles to choose
-    CUNA_TRY(time_schedule(p, t, y, F, n, t0, T, st, reps, &best));
+    s = time_schedule(p, t, y, F, n, t0, T, st, reps, flush, flush_bytes, &best);
   } else {
-    for (int method = CUNA2_GRID_GATHER; method <= CUNA2_GRID_FIXED; ++method)
-      for (int lt = 9; lt <= 13; ++lt) {
-        if (!schedule_ok(p, lt, method) || lt == logng) continue;
-        drop_graphs(p);
-        p->logTL = lt;
-        p->ntiles = (int)(p->ng >> lt);
-        p->grid_method = method;
-        float ms = 0;
-        CUNA_TRY(time_schedule(p, t, y, F, n, t0, T, st, reps, &ms));
-        if (ms < best) {
-          best = ms;
-          best_tile = lt;
-          best_method = method;
+    for (int bin = CUNA2_BIN_GLOBAL; !s && bin <= CUNA2_BIN_LOCAL; ++bin)
+      for (int method = CUNA2_GRID_GATHER; !s && method <= CUNA2_GRID_FIXED; ++method)
+        for (int lt = 9; !s && lt <= 13; ++lt) {
+          if (!schedule_ok(p, lt, method) || lt == logng) continue;
+          drop_graphs(p);
+          p->logTL = lt;
+          p->ntiles = (int)(p->ng >> lt);
+          p->grid_method = method;
+          p->binning = bin;
+          float ms = 0;
+          s = time_schedule(p, t, y, F, n, t0, T, st, reps, flush, flush_bytes, &ms);
+          if (!s && ms < best) {
+            best = ms;
+            best_tile = lt;
+            best_method = method;
+            best_bin = bin;
+          }
         }
-      }
     drop_graphs(p);
     p->logTL = best_tile;
     p->ntiles = (int)(p->ng >> best_tile);
     p->grid_method = best_method;
+    p->binning = best_bin;
   }
+  if (flush) {
+    cudaStreamSynchronize(st);
+    cudaFree(flush);
+  }
+  if (s) return s;
   if (best_ms) *best_ms = best;
+  return CUNA2_SUCCESS;
+}
+
+extern "C" int cuna2_plan_set_binning(cuna2_plan p, int mode) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  if (mode != CUNA2_BIN_GLOBAL && mode != CUNA2_BIN_LOCAL)
+    return fail(CUNA2_ERROR_INVALID_VALUE, "binning mode %d", mode);
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (mode != p->binning) drop_graphs(p);
+  p->binning = mode;
+  return CUNA2_SUCCESS;
+}
+
+extern "C" int cuna2_plan_get_binning(cuna2_plan p, int *mode) {
+  clear_error();
+  if (!p || !mode) return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
+  *mode = p->binning;
   return CUNA2_SUCCESS;
 }
 

@@ -116,6 +116,17 @@ class AdjointNFFT:
         """Tiles of 2**log_tile cells, gridded in GRID_GATHER or GRID_SCATTER form."""
         _lib.check(_lib.core().cuna2_plan_set_schedule(self._h, int(log_tile), int(grid_method)))
 
+    @property
+    def binning(self):
+        """BIN_GLOBAL or BIN_LOCAL (see cuna2_plan_set_binning)."""
+        v = ctypes.c_int()
+        _lib.check(_lib.core().cuna2_plan_get_binning(self._h, ctypes.byref(v)))
+        return v.value
+
+    @binning.setter
+    def binning(self, mode):
+        _lib.check(_lib.core().cuna2_plan_set_binning(self._h, int(mode)))
+
     def autotune(self, t, y, t0=None, T=None, reps=5, stream=None):
         """Time every admissible schedule on (t, y), keep the fastest; returns
         (log_tile, grid_method, best_ms)."""

@@ -250,12 +250,27 @@ enum { CUNA2_GRID_GATHER = 0, CUNA2_GRID_SCATTER = 1, CUNA2_GRID_FIXED = 2 };
 int cuna2_plan_set_schedule(cuna2_plan plan, int log_tile, int grid_method);
 int cuna2_plan_get_schedule(cuna2_plan plan, int *log_tile, int *grid_method);
 
+/* Bucket sort in front of the tiled gridding:
+ *   CUNA2_BIN_GLOBAL  count pass, then one pass that scans the tile counts and
+ *                     scatters the records into one tile-ordered array;
+ *   CUNA2_BIN_LOCAL   one pass: each CTA sorts a chunk of samples by tile in
+ *                     shared memory and writes runs; the gridding reads a
+ *                     tile's records as one run per chunk (used when at most
+ *                     4096 tiles and 1024 chunks of <= 16384 samples; else
+ *                     the global form runs).
+ * New plans use CUNA2_BIN_GLOBAL.  Changing it drops cached graphs. */
+enum { CUNA2_BIN_GLOBAL = 0, CUNA2_BIN_LOCAL = 1 };
+int cuna2_plan_set_binning(cuna2_plan plan, int mode);
+int cuna2_plan_get_binning(cuna2_plan plan, int *mode);
+
 /* Autotuner: runs the transform of (t, y) into F under every admissible
- * schedule with log_tile in 9..13 (below the whole grid), reps timed runs
- * each (CUDA events on `stream`, minimum taken), and keeps the fastest;
- * best_ms (may be NULL) receives its time.  Synchronises `stream`.  Plans
- * small enough for the single-CTA path have nothing to tune and keep their
- * schedule. */
+ * schedule (both binning forms, every gridding form, log_tile in 9..13 below
+ * the whole grid), reps timed runs each (CUDA events on `stream`, minimum
+ * taken, with a buffer of twice the L2 size overwritten before each run so
+ * the inputs come from HBM), and keeps the fastest; best_ms (may be NULL)
+ * receives its time.  Allocates and frees that buffer; synchronises
+ * `stream`.  Plans small enough for the single-CTA path have nothing to tune
+ * and keep their schedule. */
 int cuna2_plan_autotune(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
                         double t0, double T, cudaStream_t stream, int reps, float *best_ms);
 

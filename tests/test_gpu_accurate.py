@@ -135,8 +135,9 @@ SCHED_CASES = [
 
 @pytest.mark.parametrize("n,nf,R,m,dtype,tol", SCHED_CASES)
 def test_every_schedule(nfft, oracle_lib, n, nf, R, m, dtype, tol):
-    """Every gridding form at every admissible tile size gives the NDFT's
-    spectrum; the forms agree with each other to rounding."""
+    """Every gridding form at every admissible tile size, after either
+    binning form, gives the NDFT's spectrum; all agree with each other to
+    rounding."""
     from cunfft_adjoint_gb300 import _lib
     rng = np.random.default_rng(n)
     t = rng.uniform(0, 500.0, n)
@@ -148,18 +149,20 @@ def test_every_schedule(nfft, oracle_lib, n, nf, R, m, dtype, tol):
     sel = np.sort(rng.choice(k, 256, replace=False))
     D = oracle_lib.ndft(t, y.astype(np.float64), 0.0, 500.0, sel)
     outs = {}
-    for gm in (_lib.GRID_GATHER, _lib.GRID_SCATTER, _lib.GRID_FIXED):
-        for lt in (9, 10, 11, 12, 13):
-            if gm == _lib.GRID_GATHER and lt == 13:
-                with pytest.raises(_lib.CunaError):
-                    plan.set_schedule(lt, gm)
-                continue
-            plan.set_schedule(lt, gm)
-            assert plan.schedule == (lt, gm)
-            F = plan(td, yd, 0.0, 500.0).cpu().numpy().astype(np.complex128)
-            assert rel_l2(F[sel + nf // 2], D) < tol, (lt, gm)
-            outs[(lt, gm)] = F
-    ref = outs[(12, _lib.GRID_GATHER)]
+    for gm, lt, bn in [(g, l, b) for b in (_lib.BIN_GLOBAL, _lib.BIN_LOCAL)
+                       for g in (_lib.GRID_GATHER, _lib.GRID_SCATTER, _lib.GRID_FIXED)
+                       for l in (9, 10, 11, 12, 13)]:
+        plan.binning = bn
+        if gm == _lib.GRID_GATHER and lt == 13:
+            with pytest.raises(_lib.CunaError):
+                plan.set_schedule(lt, gm)
+            continue
+        plan.set_schedule(lt, gm)
+        assert plan.schedule == (lt, gm) and plan.binning == bn
+        F = plan(td, yd, 0.0, 500.0).cpu().numpy().astype(np.complex128)
+        assert rel_l2(F[sel + nf // 2], D) < tol, (lt, gm, bn)
+        outs[(lt, gm, bn)] = F
+    ref = outs[(12, _lib.GRID_GATHER, _lib.BIN_GLOBAL)]
     for key, F in outs.items():
         assert rel_l2(F, ref) < (2e-6 if dtype == torch.float32 else 1e-13), key
 
@@ -187,7 +190,9 @@ def test_schedules_with_slab_weights(nfft, oracle_lib, dtype):
     Y = torch.stack([yd, yd * 0 + 1, yd * yd])
     plan = nfft.AdjointNFFT(nf, R, m, dtype)
     res = []
-    for gm in (_lib.GRID_GATHER, _lib.GRID_SCATTER, _lib.GRID_FIXED):
+    for gm, bn in [(g, b) for g in (_lib.GRID_GATHER, _lib.GRID_SCATTER, _lib.GRID_FIXED)
+                   for b in (_lib.BIN_GLOBAL, _lib.BIN_LOCAL)]:
+        plan.binning = bn
         plan.set_schedule(11, gm)
         B = plan.bootstrap(td, yd, 40, 17, 0.0, 100.0).cpu().numpy()
         M = plan.multi(td, Y, 0.0, 100.0).cpu().numpy()
