@@ -249,6 +249,40 @@ def batched_legs(dev, steps):
     return out
 
 
+def autograd_leg(dev, steps):
+    """Differentiable path: a batch of 64 series (N=2e5 sorted on [0,500),
+    Nf=2^18, R=2, m=10, float32), loss sum_k w_k |F_k|^2, forward + backward
+    (dL/dt, dL/dy) per step; CUDA events, inputs resident."""
+    import torch
+    from cunfft_adjoint_gb300.autograd import BatchedAdjointNFFT
+    B, N, nf, T = 64, 200_000, 1 << 18, 500.0
+    rng = np.random.default_rng(5)
+    t = torch.as_tensor(np.sort(rng.uniform(0, T, (B, N)), axis=1), device=dev)
+    y = torch.as_tensor(rng.normal(0, 1, (B, N)).astype(np.float32), device=dev)
+    w = torch.as_tensor(rng.uniform(0, 1, (B, nf)).astype(np.float32), device=dev)
+    op = BatchedAdjointNFFT(B, N, nf, 2, 10, np.zeros(B), np.full(B, T), torch.float32, dev)
+
+    def step():
+        tt, yy = t.detach().requires_grad_(True), y.detach().requires_grad_(True)
+        F = op(tt, yy)
+        (w * (F.real ** 2 + F.imag ** 2)).sum().backward()
+        return tt.grad, yy.grad
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    k = max(3, min(20, steps // 100))
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record()
+    for _ in range(k):
+        step()
+    a1.record()
+    torch.cuda.synchronize()
+    ms = a0.elapsed_time(a1) / k
+    return {"workload": "64 series x N=2e5, Nf=2^18, R=2, m=10, loss sum w|F|^2, forward + backward (t, y)",
+            "value": B * 1000.0 / ms, "unit": "series/s (forward+backward)", "ms_per_batch": ms, "steps": k}
+
+
 def cpu_baseline(wl, budget_s=20.0):
     """The reference pipeline on the host cores (oracle CPU program)."""
     from oracle import oracle
@@ -475,6 +509,8 @@ def main():
                "steps": k64}
 
     batched = batched_legs(dev, args.steps) if rank == 0 and not args.no_side_legs else None
+    if batched is not None:
+        batched["autograd"] = autograd_leg(dev, args.steps)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
