@@ -301,15 +301,19 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   // the chunk runs of a tile sit behind the form's own shared memory
   const size_t segb = seg ? sizeof(int) * (2 * (size_t)nch + 1) : 0;
   const int ch2 = 2 * CH;
+  // gather: 8 cells per thread on tiles of 2048 cells, else 4
+  const bool cw8 = (1 << p->logTL) == 2048;
   static bool attr_done = false;
   if (!attr_done) {
     const int mx = 200 * 1024;
-    CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_fixed<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    CUNA_CK(cudaFuncSetAttribute(k_grid_acc_seg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    CUNA_CK(cudaFuncSetAttribute(k_grid_fixed_seg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    CUNA_CK(cudaFuncSetAttribute(k_grid_scatter_seg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_acc_seg<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_acc_seg<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_fixed_seg<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_scatter_seg<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     attr_done = true;
   }
   size_t smg;
@@ -317,23 +321,29 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   else if (p->grid_method == CUNA2_GRID_FIXED) smg = grid_fixed_smem_bytes<T>(p->logTL, p->m);
   else smg = grid_scatter_smem_bytes<T>(p->logTL);
   smg = (smg + 15) & ~(size_t)15;
+  const dim3 gb(kGridThreads);
   if (seg) {
-    if (p->grid_method == CUNA2_GRID_GATHER)
-      k_grid_acc_seg<T><<<ggrid, kGridThreads, smg + segb, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n,
-                                                                  nslab, group, p->ng);
-    else if (p->grid_method == CUNA2_GRID_FIXED)
-      k_grid_fixed_seg<T><<<ggrid, kGridThreads, smg + segb, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n,
-                                                                    nslab, group, p->ng);
-    else
-      k_grid_scatter_seg<T><<<ggrid, kGridThreads, smg + segb, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts,
-                                                                      n, nslab, group, p->ng);
+    const size_t sm = smg + segb;
+    if (p->grid_method == CUNA2_GRID_GATHER) {
+      if (cw8)
+        k_grid_acc_seg<T, 8><<<ggrid, gb, sm, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n, nslab, group, p->ng);
+      else
+        k_grid_acc_seg<T, 4><<<ggrid, gb, sm, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n, nslab, group, p->ng);
+    } else if (p->grid_method == CUNA2_GRID_FIXED) {
+      k_grid_fixed_seg<T, 4><<<ggrid, gb, sm, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n, nslab, group, p->ng);
+    } else {
+      k_grid_scatter_seg<T, 4><<<ggrid, gb, sm, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n, nslab, group,
+                                                     p->ng);
+    }
   } else {
-    if (p->grid_method == CUNA2_GRID_GATHER)
-      k_grid_acc<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
-    else if (p->grid_method == CUNA2_GRID_FIXED)
-      k_grid_fixed<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
-    else
-      k_grid_scatter<T><<<ggrid, kGridThreads, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+    if (p->grid_method == CUNA2_GRID_GATHER) {
+      if (cw8) k_grid_acc<T, 8><<<ggrid, gb, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+      else k_grid_acc<T, 4><<<ggrid, gb, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+    } else if (p->grid_method == CUNA2_GRID_FIXED) {
+      k_grid_fixed<T><<<ggrid, gb, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+    } else {
+      k_grid_scatter<T><<<ggrid, gb, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+    }
   }
   CUNA_CK(cudaGetLastError());
   mark(pr, "grid", st);

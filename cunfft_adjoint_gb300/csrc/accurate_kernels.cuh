@@ -275,36 +275,45 @@ template <typename T> struct __align__(2 * sizeof(T) >= 16 ? 16 : 16) SRec {
   T f, y;
   int lc, pad;
 };
-constexpr int kGridCW = 4;  // consecutive cells per thread in the gather
 
-// Weights y exp2(-k1 (x + i)^2) of one record for four consecutive cells,
-// i = 0..3.  float: four ex2.approx.  double: the fast Gaussian gridding
-// factorisation (Greengard & Lee 2004) exp2(-k1 (x+i)^2) = E Q^i c_i with
-// E = exp2(-k1 x^2), Q = exp2(-2 k1 x), c_i = exp2(-k1 i^2): two exp2 per
-// record instead of four, the FP64 pipe being the bound of the double path.
-template <typename T> struct Gauss4;
-template <> struct Gauss4<float> {
-  __device__ explicit Gauss4(float) {}
+// exp2 for the gridding weights: ex2.approx for float (relative error of a
+// few ulp), the library exp2 for double
+__device__ __forceinline__ float exp2_g(float x) { return ex2_fast(x); }
+__device__ __forceinline__ double exp2_g(double x) { return exp2(x); }
+
+// Weights y exp2(-k1 (x + i)^2) of one record for CW consecutive cells,
+// i = 0..CW-1, by the fast Gaussian gridding factorisation (Greengard & Lee
+// 2004) about the middle cell h = CW/2, xc = x + h:
+//   y exp2(-k1 (xc + j)^2) = E Q^j c_j,  E = y exp2(-k1 xc^2),
+//   Q = exp2(-2 k1 xc), c_j = exp2(-k1 j^2),
+// three exp2 per record and cell group instead of CW.  Centring keeps E and
+// the running products inside the float range for every m <= 16.
+template <typename T, int CW> struct GaussCW {
+  T c[CW / 2 + 1];
+  __device__ explicit GaussCW(T k1) {
+#pragma unroll
+    for (int j = 0; j <= CW / 2; ++j) c[j] = exp2_g(-k1 * (T)(j * j));
+  }
 };
-template <> struct Gauss4<double> {
-  double c1, c2, c3;
-  __device__ explicit Gauss4(double k1) : c1(exp2(-k1)), c2(exp2(-4.0 * k1)), c3(exp2(-9.0 * k1)) {}
-};
-__device__ __forceinline__ void gauss_w4(float y, float x, float k1, const Gauss4<float> &, float &w0, float &w1,
-                                         float &w2, float &w3) {
-  w0 = gauss_w(y, x, k1);
-  w1 = gauss_w(y, x + 1.f, k1);
-  w2 = gauss_w(y, x + 2.f, k1);
-  w3 = gauss_w(y, x + 3.f, k1);
-}
-__device__ __forceinline__ void gauss_w4(double y, double x, double k1, const Gauss4<double> &g, double &w0,
-                                         double &w1, double &w2, double &w3) {
-  const double E = y * exp2(-k1 * x * x), Q = exp2(-2.0 * k1 * x);
-  const double t1 = E * Q, t2 = t1 * Q, t3 = t2 * Q;
-  w0 = E;
-  w1 = t1 * g.c1;
-  w2 = t2 * g.c2;
-  w3 = t3 * g.c3;
+template <typename T, int CW>
+__device__ __forceinline__ void gauss_cw(T y, T x, T k1, const GaussCW<T, CW> &g, T *w) {
+  constexpr int H = CW / 2;
+  const T xc = x + (T)H;
+  const T E = y * exp2_g(-k1 * xc * xc);
+  const T Q = exp2_g((T)(-2) * k1 * xc), Qi = exp2_g((T)2 * k1 * xc);
+  w[H] = E;
+  T u = E;
+#pragma unroll
+  for (int j = 1; j < CW - H; ++j) {
+    u *= Q;
+    w[H + j] = u * g.c[j];
+  }
+  u = E;
+#pragma unroll
+  for (int j = 1; j <= H; ++j) {
+    u *= Qi;
+    w[H - j] = u * g.c[j];
+  }
 }
 
 __device__ __forceinline__ void store4(float *p, float a, float b, float c, float d) {
@@ -330,13 +339,17 @@ __device__ __forceinline__ void grid_slots(int p0, int ng, int TL, int m, int &s
 // One grid tile [base, base + 2^logTL) from records [r0, r1), for slabs
 // [sbeg, send): slab s grids value wts[s*nvals + p] of sample p when wts is
 // given (bootstrap), else the record's own value.
-template <typename T, class Src>
+// CW consecutive cells per thread in the gather (4 or 8)
+template <typename T, int CW, class Src>
 __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
                                                int base, T *__restrict__ grid, const AccParams<T> &e,
                                                const T *__restrict__ wts, int64_t nvals, int sbeg, int send,
                                                int64_t slab_stride) {
   typedef typename RecOf<T>::type Rec;
   constexpr int CAP = GridCfg<T>::CAP;
+  // cells per thread: up to 16 in groups of 4 (TL <= 4096), or one group of
+  // 8 (TL = 2048)
+  constexpr int MAXC = CW == 8 ? 8 : kGridMaxCpt;
   constexpr int RPT = CAP / kGridThreads;  // records per thread per chunk
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int TL = 1 << e.logTL, m = e.m, W = TL + 2 * m;
@@ -348,14 +361,14 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
   // a single tile spanning the whole grid maps a record to up to two slots;
   // halve the chunk then so that placements never exceed CAP
   const int chunk = (TL + 2 * m > ng) ? CAP / 2 : CAP;
-  const int npass = (TL + kGridThreads * kGridCW - 1) / (kGridThreads * kGridCW);  // <= kGridMaxCpt / kGridCW
+  const int npass = (TL + kGridThreads * CW - 1) / (kGridThreads * CW);  // <= MAXC / CW
   const int nchunks = (r1 - r0 + chunk - 1) / chunk;
-  const Gauss4<T> g4(e.k1);
+  const GaussCW<T, CW> gw(e.k1);
   // the records are sorted once for all slabs when they fit in one chunk
   for (int slab = sbeg; slab < send; ++slab) {
-    T acc[kGridMaxCpt];
+    T acc[MAXC];
 #pragma unroll
-    for (int q = 0; q < kGridMaxCpt; ++q) acc[q] = (T)0;
+    for (int q = 0; q < MAXC; ++q) acc[q] = (T)0;
     for (int ck = 0; ck < nchunks; ++ck) {
       const int c0 = r0 + ck * chunk;
       const int cnt = min(chunk, r1 - c0);
@@ -443,58 +456,58 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
         for (int i = threadIdx.x; i < placed; i += kGridThreads) srec[i].y = ws[sp[i]];
         __syncthreads();
       }
-      // gather: the thread's cells cl0 .. cl0+3 (local) take the records in
-      // slots cl0 .. cl0 + 3 + 2m - 1; record slot lc reaches cell c iff
+      // gather: the thread's cells cl0 .. cl0+CW-1 (local) take the records in
+      // slots cl0 .. cl0 + CW - 1 + 2m - 1; record slot lc reaches cell c iff
       // 0 <= lc - c < 2m
 #pragma unroll
-      for (int q = 0; q < kGridMaxCpt / kGridCW; ++q) {
-        const int cl0 = (threadIdx.x + q * kGridThreads) * kGridCW;
+      for (int q = 0; q < MAXC / CW; ++q) {
+        const int cl0 = (threadIdx.x + q * kGridThreads) * CW;
         if (q >= npass || cl0 >= TL) continue;
         const int rb = cl0 == 0 ? 0 : start[cl0 - 1];
-        const int re = start[cl0 + kGridCW - 1 + 2 * m - 1];
-        T a0 = (T)0, a1 = (T)0, a2 = (T)0, a3 = (T)0;
+        const int re = start[cl0 + CW - 1 + 2 * m - 1];
+        T a[CW];
+#pragma unroll
+        for (int i = 0; i < CW; ++i) a[i] = (T)0;
         const int ctr = cl0 + m;
+        const unsigned w2 = (unsigned)(2 * m);
         for (int r = rb; r < re; ++r) {
           const SRec<T> rr = srec[r];
-          const int rel = rr.lc - cl0;                 // lc - c for c = cl0
-          const T dd0 = (T)(ctr - rr.lc) - rr.f;       // d - f for c = cl0
-          const unsigned w2 = (unsigned)(2 * m);
-          T w0, w1, wq2, w3;
-          gauss_w4(rr.y, dd0, e.k1, g4, w0, w1, wq2, w3);
-          a0 += (unsigned)rel < w2 ? w0 : (T)0;
-          a1 += (unsigned)(rel - 1) < w2 ? w1 : (T)0;
-          a2 += (unsigned)(rel - 2) < w2 ? wq2 : (T)0;
-          a3 += (unsigned)(rel - 3) < w2 ? w3 : (T)0;
+          const int rel = rr.lc - cl0;            // lc - c for c = cl0
+          const T dd0 = (T)(ctr - rr.lc) - rr.f;  // d - f for c = cl0
+          T w[CW];
+          gauss_cw<T, CW>(rr.y, dd0, e.k1, gw, w);
+#pragma unroll
+          for (int i = 0; i < CW; ++i) a[i] += (unsigned)(rel - i) < w2 ? w[i] : (T)0;
         }
-        acc[4 * q + 0] += a0;
-        acc[4 * q + 1] += a1;
-        acc[4 * q + 2] += a2;
-        acc[4 * q + 3] += a3;
+#pragma unroll
+        for (int i = 0; i < CW; ++i) acc[CW * q + i] += a[i];
       }
       __syncthreads();
     }
     T *out = grid + (int64_t)slab * slab_stride + base;
 #pragma unroll
-    for (int q = 0; q < kGridMaxCpt / kGridCW; ++q) {
-      const int cl0 = (threadIdx.x + q * kGridThreads) * kGridCW;
-      // TL is a power of two >= 4 (ng >= 4m >= 4), so every group of four
-      // cells is whole and the vector store stays inside the tile
+    for (int q = 0; q < MAXC / CW; ++q) {
+      const int cl0 = (threadIdx.x + q * kGridThreads) * CW;
+      // TL is a power of two >= CW (gather tiles have >= 512 cells or span the
+      // grid, ng >= 4m >= 4 and CW = 4 there), so groups are whole
       if (q < npass && cl0 < TL) {
-        store4(out + cl0, acc[4 * q + 0], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+#pragma unroll
+        for (int i = 0; i < CW; i += 4)
+          store4(out + cl0 + i, acc[CW * q + i], acc[CW * q + i + 1], acc[CW * q + i + 2], acc[CW * q + i + 3]);
       }
     }
   }
 }
 
-template <typename T>
+template <typename T, int CW>
 __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 4 : 2) k_grid_acc(
     const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
     AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab, int group, int64_t slab_stride) {
   // a CTA per (tile, group of slabs)
   const int tile = blockIdx.x;
   const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
-  grid_tile_body<T>(recs, off[tile], off[tile + 1], tile << e.logTL, grid, e, wts, nvals, sbeg, send,
-                    slab_stride);
+  grid_tile_body<T, CW>(recs, off[tile], off[tile + 1], tile << e.logTL, grid, e, wts, nvals, sbeg, send,
+                        slab_stride);
 }
 
 // Scatter form of the same tile gridding: the tile's cells accumulate in
@@ -601,11 +614,6 @@ template <> struct FixAcc<double> {
     atomicAdd(reinterpret_cast<unsigned long long *>(a), (unsigned long long)v);
   }
 };
-
-// exp2 for the gridding weights: ex2.approx for float (relative error of a
-// few ulp), the library exp2 for double
-__device__ __forceinline__ float exp2_g(float x) { return ex2_fast(x); }
-__device__ __forceinline__ double exp2_g(double x) { return exp2(x); }
 
 // records [c0, c0 + cnt) -> srec (values from ws when given); returns the
 // thread's max |value| (NaN once one is not finite)
@@ -816,7 +824,7 @@ __device__ __forceinline__ int seg_setup(const int *__restrict__ loc, int tile, 
 }
 
 #define CUNA_SEG_KERNEL(NAME, BODY, OCC32, OCC64)                                                              \
-  template <typename T>                                                                                       \
+  template <typename T, int CW>                                                                               \
   __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? OCC32 : OCC64) NAME(                        \
       const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ loc, int nch, int ch2,          \
       int seg_off, T *__restrict__ grid, AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab,    \
@@ -827,11 +835,11 @@ __device__ __forceinline__ int seg_setup(const int *__restrict__ loc, int tile, 
     const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);                                       \
     const int total = seg_setup(loc, tile, nch, ch2, sh);                                                       \
     const SegSrc<T> src{recs, sh, sh + nch + 1, nch};                                                           \
-    BODY<T>(src, 0, total, tile << e.logTL, grid, e, wts, nvals, sbeg, send, slab_stride);                       \
+    BODY(src, 0, total, tile << e.logTL, grid, e, wts, nvals, sbeg, send, slab_stride);                          \
   }
-CUNA_SEG_KERNEL(k_grid_acc_seg, grid_tile_body, 4, 2)
-CUNA_SEG_KERNEL(k_grid_scatter_seg, grid_tile_scatter, 6, 3)
-CUNA_SEG_KERNEL(k_grid_fixed_seg, grid_tile_fixed, 6, 2)
+CUNA_SEG_KERNEL(k_grid_acc_seg, (grid_tile_body<T, CW>), 4, 2)
+CUNA_SEG_KERNEL(k_grid_scatter_seg, grid_tile_scatter<T>, 6, 3)
+CUNA_SEG_KERNEL(k_grid_fixed_seg, grid_tile_fixed<T>, 6, 2)
 #undef CUNA_SEG_KERNEL
 
 template <typename T> size_t grid_scatter_smem_bytes(int logTL) {

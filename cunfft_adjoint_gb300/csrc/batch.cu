@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 4 : 2) k_bgrid(
     const BDesc<T> *__restrict__ D, const int *__restrict__ tile_series) {
   const int gt = blockIdx.x;
   const BDesc<T> d = D[tile_series[gt]];
-  grid_tile_body<T>(recs, off[gt], off[gt + 1], (gt - d.tile0) << d.e.logTL, grid + d.g_off, d.e, nullptr, 0, 0, 1,
+  grid_tile_body<T, 4>(recs, off[gt], off[gt + 1], (gt - d.tile0) << d.e.logTL, grid + d.g_off, d.e, nullptr, 0, 0, 1,
                     0);
 }
 
