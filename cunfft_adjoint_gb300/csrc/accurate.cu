@@ -42,6 +42,11 @@ struct cuna2_plan_st {
   int grid_method = CUNA2_GRID_GATHER;  // tile gridding form (cuna2_plan_set_schedule)
   int binning = CUNA2_BIN_GLOBAL;      // bucket sort form (cuna2_plan_set_binning)
   bool small;  // single-CTA fused path
+  // small plans with a multi-CTA four-step instance: a single transform may
+  // run tiled (binning, tiled gridding, two FFT passes) instead
+  bool has_split = false;
+  bool tiled_single = true;
+  cuna::FftGeom geom4;
   cuna::FftGeom geom;
   int device;
   std::mutex mu;
@@ -153,9 +158,9 @@ int ct_passes(int logL, typename CxOf<T>::type *z, const FftDev<T> &f, const Acc
 #define CUNA_CT(LG) \
   case LG: return ct_passes_at<T, LG>(z, f, e, F, nslab, st, pr);
   if constexpr (sizeof(T) == 4) {
-    switch (logL) { CUNA_CT(15) CUNA_CT(16) CUNA_CT(17) CUNA_CT(18) CUNA_CT(19) CUNA_CT(20) CUNA_CT(21) CUNA_CT(22) CUNA_CT(23) CUNA_CT(24) CUNA_CT(25) }
+    switch (logL) { CUNA_CT(13) CUNA_CT(14) CUNA_CT(15) CUNA_CT(16) CUNA_CT(17) CUNA_CT(18) CUNA_CT(19) CUNA_CT(20) CUNA_CT(21) CUNA_CT(22) CUNA_CT(23) CUNA_CT(24) CUNA_CT(25) }
   } else {
-    switch (logL) { CUNA_CT(14) CUNA_CT(15) CUNA_CT(16) CUNA_CT(17) CUNA_CT(18) CUNA_CT(19) CUNA_CT(20) CUNA_CT(21) CUNA_CT(22) CUNA_CT(23) }
+    switch (logL) { CUNA_CT(12) CUNA_CT(13) CUNA_CT(14) CUNA_CT(15) CUNA_CT(16) CUNA_CT(17) CUNA_CT(18) CUNA_CT(19) CUNA_CT(20) CUNA_CT(21) CUNA_CT(22) CUNA_CT(23) }
   }
 #undef CUNA_CT
   return 0;
@@ -184,7 +189,9 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   const int nslab = multi ? nmulti : (nbs > 0 ? nbs : 1);
   const PhaseMul pm = phase_setup(t0, T_);
   const AccParams<T> e = make_params<T>(p);
-  const FftDev<T> f = to_dev<T>(p->geom);
+  // one transform of a small plan runs tiled over many CTAs when it can
+  const bool small = p->small && !(p->has_split && p->tiled_single && nslab == 1);
+  const FftDev<T> f = to_dev<T>(small || !p->small ? p->geom : p->geom4);
   const int L = 1 << p->geom.logL;
   const int ntiles = p->ntiles;
   // binning: single pass into chunk-local tile order (k_bin_local) when the
@@ -192,7 +199,7 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   // Chunks of CH samples: at least two per SM, at most kSegMaxChunks.
   const int nsm = device_sm_count();
   int CH = 0, nch = 0;
-  if (p->binning == CUNA2_BIN_LOCAL && !p->small && n > 0 && ntiles <= kScanFuseTiles) {
+  if (p->binning == CUNA2_BIN_LOCAL && !small && n > 0 && ntiles <= kScanFuseTiles) {
     int64_t want = std::max<int64_t>(std::max<int64_t>((n + 2 * nsm - 1) / (2 * nsm),
                                                        (n + kSegMaxChunks - 1) / kSegMaxChunks), 1024);
     want = (want + 511) / 512 * 512;
@@ -206,11 +213,11 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   const size_t o_cnt = 0, o_cur = align_up(sizeof(int) * ntiles), o_off = 2 * o_cur;
   const size_t o_phs = o_off + align_up(sizeof(int) * (ntiles + 1));
   const size_t nrec = seg ? 2 * ((size_t)n + CH) : 2 * (size_t)(n > 0 ? n : 1);
-  const size_t o_rec = o_phs + (p->small ? 0
+  const size_t o_rec = o_phs + (small ? 0
                                          : (seg ? align_up(sizeof(int) * (size_t)ntiles * nch)
                                                 : align_up(sizeof(uint64_t) * (size_t)(n > 0 ? n : 1))));
-  const size_t o_grid = o_rec + (p->small ? 0 : align_up(sizeof(Rec) * nrec));
-  const size_t o_wts = o_grid + (p->small ? 0 : align_up(sizeof(T) * (size_t)p->ng * nslab));
+  const size_t o_grid = o_rec + (small ? 0 : align_up(sizeof(Rec) * nrec));
+  const size_t o_wts = o_grid + (small ? 0 : align_up(sizeof(T) * (size_t)p->ng * nslab));
   const size_t bytes = o_wts + (nbs > 0 ? sizeof(T) * (size_t)n * nbs : 0) + 256;
   void *ws = nullptr;
   CUNA_TRY(plan_workspace(p, bytes, &ws));
@@ -235,7 +242,7 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     CUNA_CK(cudaGetLastError());
     mark(pr, "boot_weights", st);
   }
-  if (p->small) {
+  if (small) {
     static bool attr = false;
     if (!attr) {
       CUNA_CK(cudaFuncSetAttribute(k_nfft_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
@@ -413,6 +420,11 @@ extern "C" int cuna2_plan_create(cuna2_plan *plan, int dtype, int64_t nf, int R,
   cudaGetDevice(&p->device);
   int st = fft_geometry(dtype == CUNA2_F64, logL, &p->geom);
   if (st) {
+    delete p;
+    return st;
+  }
+  p->has_split = p->small && logL >= (dtype == CUNA2_F32 ? 13 : 12);
+  if (p->has_split && (st = fft_geometry(dtype == CUNA2_F64, logL, &p->geom4, true))) {
     delete p;
     return st;
   }
@@ -639,6 +651,7 @@ extern "C" int cuna2_plan_autotune(cuna2_plan p, const double *t, const void *y,
   std::lock_guard<std::mutex> lk(p->mu);
   const int logng = ilog2i(p->ng);
   int best_tile = p->logTL, best_method = p->grid_method, best_bin = p->binning;
+  bool best_tiled = p->tiled_single;
   float best = 3.4e38f;
   // a buffer of twice the L2 size, overwritten before each timed run
   int dev = 0, l2 = 0;
@@ -651,9 +664,15 @@ extern "C" int cuna2_plan_autotune(cuna2_plan p, const double *t, const void *y,
     flush = nullptr;
   }
   int s = CUNA2_SUCCESS;
-  if (p->small) {  // one fused CTA per transform: no tiles to choose
+  if (p->small) {  // the single-CTA path: no tiles to choose
+    const bool keep = p->tiled_single;
+    p->tiled_single = false;
     s = time_schedule(p, t, y, F, n, t0, T, st, reps, flush, flush_bytes, &best);
-  } else {
+    p->tiled_single = keep;
+    best_tiled = false;
+  }
+  if (!s && (!p->small || p->has_split)) {  // tiled schedules
+    p->tiled_single = true;
     for (int bin = CUNA2_BIN_GLOBAL; !s && bin <= CUNA2_BIN_LOCAL; ++bin)
       for (int method = CUNA2_GRID_GATHER; !s && method <= CUNA2_GRID_FIXED; ++method)
         for (int lt = 9; !s && lt <= 13; ++lt) {
@@ -670,14 +689,16 @@ extern "C" int cuna2_plan_autotune(cuna2_plan p, const double *t, const void *y,
             best_tile = lt;
             best_method = method;
             best_bin = bin;
+            best_tiled = true;
           }
         }
-    drop_graphs(p);
-    p->logTL = best_tile;
-    p->ntiles = (int)(p->ng >> best_tile);
-    p->grid_method = best_method;
-    p->binning = best_bin;
   }
+  drop_graphs(p);
+  p->logTL = best_tile;
+  p->ntiles = (int)(p->ng >> best_tile);
+  p->grid_method = best_method;
+  p->binning = best_bin;
+  p->tiled_single = best_tiled;
   if (flush) {
     cudaStreamSynchronize(st);
     cudaFree(flush);

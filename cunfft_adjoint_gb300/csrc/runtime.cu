@@ -112,12 +112,12 @@ int upload_table(int64_t count, int64_t step_num, int64_t denom, const void **ou
 }
 }  // namespace
 
-int fft_geometry(bool is_double, int logL, FftGeom *g) {
+int fft_geometry(bool is_double, int logL, FftGeom *g, bool split) {
   if (logL < 0 || logL > kMaxLogL) return fail(CUNA2_ERROR_UNSUPPORTED, "FFT length 2^%d unsupported", logL);
   int dev = 0;
   CUNA_CK(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lk(g_tw_mu);
-  auto key = std::make_tuple(dev, is_double ? 1 : 0, logL);
+  auto key = std::make_tuple(dev, (is_double ? 1 : 0) + (split ? 2 : 0), logL);
   auto it = g_tw->find(key);
   if (it != g_tw->end()) {
     *g = it->second.g;
@@ -126,7 +126,7 @@ int fft_geometry(bool is_double, int logL, FftGeom *g) {
   FftGeom G{};
   G.logL = logL;
   const int single_log = is_double ? kSingleLogF64 : kSingleLogF32;
-  G.single = logL <= single_log;
+  G.single = logL <= single_log && !split;
   if (G.single) {
     G.logL1 = logL;
     G.logL2 = 0;

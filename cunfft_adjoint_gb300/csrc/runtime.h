@@ -54,6 +54,8 @@ constexpr int kMaxLogL = 26;
 // host, rounded once to the element type, cached per device).  `min_rows`
 // forces the row pass to hold at least that many rows (2 for the real-input
 // unpack, which pairs rows k1 and L1-k1).
-int fft_geometry(bool is_double, int logL, FftGeom *g);
+// split: force the four-step L1 x L2 factorisation even where one CTA could
+// hold the whole transform (multi-CTA passes for a single small transform)
+int fft_geometry(bool is_double, int logL, FftGeom *g, bool split = false);
 
 }  // namespace cuna

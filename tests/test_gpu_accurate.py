@@ -206,11 +206,13 @@ def test_schedules_with_slab_weights(nfft, oracle_lib, dtype):
     assert rel_l2(res[1][1][1][::64], D) < (1e-5 if dtype == torch.float32 else 2e-9)
 
 
-@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
-def test_autotune(nfft, oracle_lib, dtype):
+@pytest.mark.parametrize("dtype,n,nf", [(torch.float32, 300_000, 1 << 18), (torch.float64, 300_000, 1 << 18),
+                                        (torch.float32, 10_000, 1 << 14), (torch.float64, 8_000, 1 << 13)])
+def test_autotune(nfft, oracle_lib, dtype, n, nf):
+    """Autotuned plans (large: tiles x forms x binning; small: also the
+    single-CTA path) still give the NDFT's spectrum."""
     from cunfft_adjoint_gb300 import _lib
     rng = np.random.default_rng(11)
-    n, nf = 300_000, 1 << 18
     t = rng.uniform(0, 1000.0, n)
     y = rng.normal(0, 1, n)
     td = torch.as_tensor(t, device="cuda")
