@@ -203,7 +203,7 @@ __device__ __forceinline__ void cta_exclusive_scan(const int *in, int *out, int 
 // k_bin_scan_scatter: k_scan_tiles folded into k_bin_scatter.  Every CTA
 // scans the tile counts itself (ntiles <= kScanFuseTiles ints, from L2) and
 // CTA 0 also publishes offsets[0..ntiles] for the gridding.  cursor[] must be
-// zero on entry.
+// zero on entry.  Launched with 512 threads.
 constexpr int kScanFuseTiles = 4096;  // 3 shared arrays of ntiles ints: 48 KB
 
 template <class S>
@@ -213,9 +213,14 @@ __global__ void __launch_bounds__(512) k_bin_scan_scatter(S smp, const int *__re
   typedef typename S::Rec Rec;
   extern __shared__ int sh[];
   int *lc = sh, *lbase = sh + ntiles, *off = sh + 2 * ntiles;  // off: ntiles + 1
-  for (int t = threadIdx.x; t < ntiles; t += blockDim.x) {
-    lc[t] = 0;
-    lbase[t] = counts[t];
+  constexpr int TPT = kScanFuseTiles / 512;  // tiles per thread (blockDim 512)
+#pragma unroll
+  for (int k = 0; k < TPT; ++k) {
+    const int t = threadIdx.x + k * 512;
+    if (t < ntiles) {
+      lc[t] = 0;
+      lbase[t] = counts[t];
+    }
   }
   __syncthreads();
   cta_exclusive_scan(lbase, off, ntiles);
@@ -238,8 +243,20 @@ __global__ void __launch_bounds__(512) k_bin_scan_scatter(S smp, const int *__re
     for (int q = 0; q < p[it].nt; ++q) rk[it][q] = atomicAdd(&lc[p[it].t[q]], 1);
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < ntiles; t += blockDim.x)
-    if (lc[t]) lbase[t] = off[t] + atomicAdd(&cursor[t], lc[t]);
+  // one reservation per touched tile; all of a thread's reservations are in
+  // flight together before any result is used
+  int res[TPT];
+#pragma unroll
+  for (int k = 0; k < TPT; ++k) {
+    const int t = threadIdx.x + k * 512;
+    const int c = t < ntiles ? lc[t] : 0;
+    res[k] = c ? atomicAdd(&cursor[t], c) : 0;
+  }
+#pragma unroll
+  for (int k = 0; k < TPT; ++k) {
+    const int t = threadIdx.x + k * 512;
+    if (t < ntiles && lc[t]) lbase[t] = off[t] + res[k];
+  }
   __syncthreads();
 #pragma unroll
   for (int it = 0; it < kScatterItems; ++it)
