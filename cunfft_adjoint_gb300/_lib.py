@@ -67,6 +67,7 @@ CORE_SIGNATURES = {
     "cuna2_plan_info": (_I, [_P, _P, _P]),
     "cuna2_adjoint": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P]),
     "cuna2_adjoint_host": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P]),
+    "cuna2_adjoint_host_async": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P]),
     "cuna2_adjoint_bootstrap": (_I, [_P, _P, _P, _P, _I64, _I, _U, _D, _D, _P]),
     "cuna2_adjoint_backward": (_I, [_P, _P, _P, _P, _P, _P, _I64, _D, _D, _P]),
     "cuna2_adjoint_multi": (_I, [_P, _P, _P, _P, _I64, _I, _D, _D, _P]),

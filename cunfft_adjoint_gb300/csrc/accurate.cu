@@ -520,9 +520,29 @@ extern "C" int cuna2_plan_set_graph(cuna2_plan p, int enable) {
   return CUNA2_SUCCESS;
 }
 
+namespace cuna {
+namespace {
+int host_run(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0, double T,
+             cudaStream_t st, bool sync);
+}
+}  // namespace cuna
+
 extern "C" int cuna2_adjoint_host(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0,
                                   double T, cudaStream_t st) {
   clear_error();
+  return host_run(p, t, y, F, n, t0, T, st, true);
+}
+
+extern "C" int cuna2_adjoint_host_async(cuna2_plan p, const double *t, const void *y, void *F, int64_t n,
+                                        double t0, double T, cudaStream_t st) {
+  clear_error();
+  return host_run(p, t, y, F, n, t0, T, st, false);
+}
+
+namespace cuna {
+namespace {
+int host_run(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0, double T,
+             cudaStream_t st, bool sync) {
   if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
   if (n < 0 || (n > 0 && (!t || !y)) || !F) return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
   std::lock_guard<std::mutex> lk(p->mu);
@@ -549,9 +569,11 @@ extern "C" int cuna2_adjoint_host(cuna2_plan p, const double *t, const void *y, 
   }
   CUNA_TRY(p->use_graph ? run_graph(p, td, yd, Fd, n, t0, T, st) : run_any(p, td, yd, Fd, n, t0, T, st, nullptr));
   CUNA_CK(cudaMemcpyAsync(F, Fd, bF, cudaMemcpyDeviceToHost, st));
-  CUNA_CK(cudaStreamSynchronize(st));
+  if (sync) CUNA_CK(cudaStreamSynchronize(st));
   return CUNA2_SUCCESS;
 }
+}  // namespace
+}  // namespace cuna
 
 extern "C" int cuna2_plan_profile(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0,
                                   double T, cudaStream_t st, float *stage_ms, const char **stage_names,

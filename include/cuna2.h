@@ -214,6 +214,17 @@ int cuna2_adjoint_backward(cuna2_plan plan, const double *t, const void *y, cons
 int cuna2_adjoint_host(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
                        double t0, double T, cudaStream_t stream);
 
+/* The same without the final synchronisation: copies in, transform and copy
+ * out are only enqueued on `stream`, so a caller that streams many series
+ * through two plans on two streams overlaps one series' transfers with the
+ * other's transform (the replacement, with host arrays, for the reference's
+ * cunfft_adjoint_raw_async, src/cuna_kernel.cu:181-223).  t, y and F must be
+ * pinned and stay untouched until the stream reaches the end of the call;
+ * one plan must not be used on two streams at once (its staging and
+ * workspace are shared). */
+int cuna2_adjoint_host_async(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
+                             double t0, double T, cudaStream_t stream);
+
 /* enable != 0: cuna2_adjoint / cuna2_adjoint_host capture their launch
  * sequence into a CUDA graph the first time they see an argument set
  * (pointers, n, t0, T) and replay it afterwards (up to 8 cached sets).  The
