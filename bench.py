@@ -381,6 +381,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--streams", type=int, default=3, help="concurrent streams, one plan each")
     ap.add_argument("--no-side-legs", action="store_true", help="skip the float64 and batched legs")
     ap.add_argument("--nsets", type=int, default=NSETS, help="rotating input sets (default 16: 192 MB > L2)")
     args = ap.parse_args()
@@ -401,39 +402,64 @@ def main():
     ts, ys = make_inputs(wl, 1000 + rank, nsets)
     td = [torch.as_tensor(t, dtype=torch.float64, device=dev) for t in ts]
     yd = [torch.as_tensor(y.astype(np.float32), device=dev) for y in ys]
-    Fd = [torch.empty(nf, dtype=torch.complex64, device=dev) for _ in range(4)]
+    nstr = max(1, args.streams)
+    Fd = [torch.empty(nf, dtype=torch.complex64, device=dev) for _ in range(nstr)]
     plan = AdjointNFFT(nf, R, m, torch.float32, device=dev)
     L = _lib.core()
     # the plan's own autotuner picks the tile size and gridding form on input set 0
     schedule = plan.autotune(td[0], yd[0], 0.0, T, reps=5)[:2] if not args.no_autotune else plan.schedule
+    # independent series stream through one plan per CUDA stream (a plan's
+    # workspace serves one stream at a time); the others copy the schedule
+    plans = [plan] + [AdjointNFFT(nf, R, m, torch.float32, device=dev) for _ in range(nstr - 1)]
+    streams = [torch.cuda.current_stream(dev)] + [torch.cuda.Stream(dev) for _ in range(nstr - 1)]
+    for p_ in plans[1:]:
+        _lib.check(L.cuna2_plan_set_schedule(p_._h, *plan.schedule))
+        _lib.check(L.cuna2_plan_set_binning(p_._h, plan.binning))
     if not args.no_graph:
-        _lib.check(L.cuna2_plan_set_graph(plan._h, 1))
-    stream = torch.cuda.current_stream(dev)
+        for p_ in plans:
+            _lib.check(L.cuna2_plan_set_graph(p_._h, 1))
+    stream = streams[0]
 
-    def step(s):
-        plan.adjoint(td[s % nsets], yd[s % nsets], 0.0, T, out=Fd[s % 4])
+    def step(s, ns=nstr):
+        k = s % ns
+        _lib.check(L.cuna2_adjoint(plans[k]._h, td[s % nsets].data_ptr(), yd[s % nsets].data_ptr(),
+                                   Fd[k].data_ptr(), n, 0.0, T, streams[k].cuda_stream))
 
-    for s in range(max(args.warmup, 3) + nsets):  # every input set gets its graph before timing
+    # every (plan, input set) pair gets its graph before timing
+    for s in range(max(args.warmup, 3) + nsets * nstr):
         step(s)
+    for s in range(nsets):
+        step(s, 1)
     torch.cuda.synchronize()
     # accuracy of one output against a direct FP64 sum
     err = ndft_check(ts[0], ys[0].astype(np.float32), plan.adjoint(td[0], yd[0], 0.0, T).cpu().numpy(), nf, T)
 
+    def timed(ns, k):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(streams[0])
+        for st in streams[1:ns]:
+            st.wait_event(e0)
+        for s in range(k):
+            step(s, ns)
+        for st in streams[1:ns]:
+            ev = torch.cuda.Event()
+            ev.record(st)
+            streams[0].wait_event(ev)
+        e1.record(streams[0])
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
-        e0.record(stream)
-        for s in range(args.steps):
-            step(s)
-        e1.record(stream)
-        torch.cuda.synchronize()
-    ms = max_over_ranks(e0.elapsed_time(e1), ws, dev)
+        ms = timed(nstr, args.steps)
+    ms = max_over_ranks(ms, ws, dev)
     if ws > 1:
         torch.distributed.barrier()
     ms_step = ms / args.steps
     value = replica_value(ms, args.steps, ws)
+    ms1 = timed(1, args.steps) / args.steps  # one stream: the per-transform latency
 
     # per-launch durations (CUDA events between launches on the plan's stream)
     import ctypes
@@ -462,39 +488,36 @@ def main():
 
     # e2e: the same transforms through the host-buffer C-ABI entry from pinned
     # host arrays, H2D copy of t, y and D2H copy of F inside every step: a
-    # stream of series alternating over two plans on two streams
-    # (cuna2_adjoint_host_async), so one series' copies overlap the other's
+    # stream of series spread over the same plans and streams
+    # (cuna2_adjoint_host_async), so one series' copies overlap another's
     # transform, as a caller streaming many series would run it
     th = [torch.as_tensor(t).pin_memory() for t in ts[:4]]
     yh = [torch.as_tensor(y.astype(np.float32)).pin_memory() for y in ys[:4]]
     nh = len(th)
-    Fh = [torch.empty(nf, dtype=torch.complex64).pin_memory() for _ in range(2)]
     e2e_steps = max(1, min(args.steps, 200))
-    plan_b = AdjointNFFT(nf, R, m, torch.float32, device=dev)
-    _lib.check(L.cuna2_plan_set_schedule(plan_b._h, *plan.schedule))
-    _lib.check(L.cuna2_plan_set_binning(plan_b._h, plan.binning))
-    if not args.no_graph:
-        _lib.check(L.cuna2_plan_set_graph(plan_b._h, 1))
-    streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
-    hplans = [plan, plan_b]
+    hplans, hstreams = plans, streams
+    nh2 = nstr
+    Fh = [torch.empty(nf, dtype=torch.complex64).pin_memory() for _ in range(nh2)]
 
     def host_step(s):
-        k = s % 2
+        k = s % nh2
         _lib.check(L.cuna2_adjoint_host_async(hplans[k]._h, th[s % nh].data_ptr(), yh[s % nh].data_ptr(),
-                                              Fh[k].data_ptr(), n, 0.0, T, streams[k].cuda_stream))
+                                              Fh[k].data_ptr(), n, 0.0, T, hstreams[k].cuda_stream))
 
     for s in range(8):
         host_step(s)
     torch.cuda.synchronize()
     h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    h0.record(streams[0])
-    streams[1].wait_event(h0)
+    h0.record(hstreams[0])
+    for st in hstreams[1:]:
+        st.wait_event(h0)
     for s in range(e2e_steps):
         host_step(s)
-    j1 = torch.cuda.Event()
-    j1.record(streams[1])
-    streams[0].wait_event(j1)
-    h1.record(streams[0])
+    for st in hstreams[1:]:
+        j1 = torch.cuda.Event()
+        j1.record(st)
+        hstreams[0].wait_event(j1)
+    h1.record(hstreams[0])
     torch.cuda.synchronize()
     e2e_ms = h0.elapsed_time(h1) / e2e_steps
     # the blocking single-call form, for reference
@@ -552,9 +575,11 @@ def main():
                        "cache": "%d rotating input sets (%.0f MB of t,y; L2 is 129 MB)" %
                                 (nsets, nsets * n * 12 / 1e6),
                        "graph": not args.no_graph, "parallelism": "replicas" if ws > 1 else "single",
+                       "streams": nstr,
                        "schedule": {"log_tile": schedule[0],
                                     "grid_method": ["gather", "scatter", "fixed"][schedule[1]]}},
             "rel_err_vs_fp64_ndft": err,
+            "single_stream": {"value": ws * 1000.0 / ms1, "ms_per_step": ms1},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
                          "traffic": traffic, "algorithmic_bytes": sb.get(dom, 0)},
@@ -562,7 +587,7 @@ def main():
             "pipeline_gbs": total_bytes / (ms_step * 1e-3) / 1e9,
             "e2e": {"value": 1000.0 / e2e_ms, "unit": UNIT, "ms_per_step": e2e_ms, "steps": e2e_steps,
                     "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": nf * 8,
-                    "api": "cuna2_adjoint_host_async, two plans on two streams, pinned host buffers",
+                    "api": "cuna2_adjoint_host_async, one plan per stream, %d streams, pinned host buffers" % nstr,
                     "blocking_call_ms": blocking_ms},
             "gpu_launches": kernels_per_step * args.steps,
             "clocks": clk.summary(),
