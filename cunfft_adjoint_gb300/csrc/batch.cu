@@ -22,6 +22,7 @@
 #include <mutex>
 #include <vector>
 #include "accurate_kernels.cuh"
+#include "fftpass.cuh"
 
 namespace cuna {
 namespace {
@@ -140,6 +141,61 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_browpass(const T
   rowpass_acc_body<T>(reinterpret_cast<const C *>(grid + d.g_off), d.f, d.e, F + d.f_off, it.a);
 }
 
+// Four-step passes with compile-time geometry for one size class of large
+// series: blockIdx.y indexes the class's series list.
+template <typename T, int LOGL>
+__global__ void __launch_bounds__(PassCfg<T>::THREADS) k_bct_colpass(T *grid, const BDesc<T> *__restrict__ D,
+                                                                     const int *__restrict__ list) {
+  typedef typename CxOf<T>::type C;
+  const int s = list[blockIdx.y];
+  ct_colpass_body<T, LOGL>(reinterpret_cast<C *>(grid + D[s].g_off), D[s].f, blockIdx.x);
+}
+
+template <typename T, int LOGL>
+__global__ void __launch_bounds__(PassCfg<T>::THREADS) k_bct_rowpass(const T *grid, const BDesc<T> *__restrict__ D,
+                                                                     const int *__restrict__ list,
+                                                                     typename CxOf<T>::type *F) {
+  typedef typename CxOf<T>::type C;
+  const int s = list[blockIdx.y];
+  ct_rowpass_body<T, LOGL>(reinterpret_cast<const C *>(grid + D[s].g_off), D[s].f, D[s].e, F + D[s].f_off,
+                           blockIdx.x);
+}
+
+template <typename T, int LOGL>
+int bct_at(T *grid, const BDesc<T> *D, const int *list, int cnt, typename CxOf<T>::type *F, cudaStream_t st) {
+  constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
+  constexpr int BA = PassCfg<T>::ELEMS >> LOG1, BB = PassCfg<T>::ELEMS >> LOG2, PB = BB / 2;
+  constexpr int npairs = (1 << LOG1) / 2 + 1;
+  constexpr size_t smA = ct_colpass_smem<T, LOGL>(), smB = ct_rowpass_smem<T, LOGL>();
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(k_bct_colpass<T, LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smA) ||
+        cudaFuncSetAttribute(k_bct_rowpass<T, LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smB))
+      return -1;
+    attr = true;
+  }
+  k_bct_colpass<T, LOGL><<<dim3((1 << LOG2) / BA, cnt), PassCfg<T>::THREADS, smA, st>>>(grid, D, list);
+  if (cudaPeekAtLastError() != cudaSuccess) return -1;
+  k_bct_rowpass<T, LOGL><<<dim3((npairs + PB - 1) / PB, cnt), PassCfg<T>::THREADS, smB, st>>>(grid, D, list, F);
+  if (cudaPeekAtLastError() != cudaSuccess) return -1;
+  return 1;
+}
+
+// 1: launched, 0: no compiled instance for logL, -1: launch error
+template <typename T>
+int bct_passes(int logL, T *grid, const BDesc<T> *D, const int *list, int cnt, typename CxOf<T>::type *F,
+               cudaStream_t st) {
+#define CUNA_BCT(LG) \
+  case LG: return bct_at<T, LG>(grid, D, list, cnt, F, st);
+  if constexpr (sizeof(T) == 4) {
+    switch (logL) { CUNA_BCT(15) CUNA_BCT(16) CUNA_BCT(17) CUNA_BCT(18) CUNA_BCT(19) CUNA_BCT(20) CUNA_BCT(21) CUNA_BCT(22) CUNA_BCT(23) CUNA_BCT(24) CUNA_BCT(25) }
+  } else {
+    switch (logL) { CUNA_BCT(14) CUNA_BCT(15) CUNA_BCT(16) CUNA_BCT(17) CUNA_BCT(18) CUNA_BCT(19) CUNA_BCT(20) CUNA_BCT(21) CUNA_BCT(22) CUNA_BCT(23) }
+  }
+#undef CUNA_BCT
+  return 0;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512) k_bsmall(const double *__restrict__ t,
                                                                         const T *__restrict__ y,
@@ -210,6 +266,11 @@ struct cuna2_batch_plan_st {
   // small series by grid size class (log2 of the packed length)
   std::vector<std::pair<int, int>> small_classes;  // (logL, count)
   std::vector<int> small_class_off;
+  // large series by packed length (log2), for the compile-time FFT passes
+  std::vector<std::pair<int, int>> fft_classes;  // (logL, count)
+  std::vector<int> fft_class_off;
+  bool fft_ct = false;  // every class has a compiled instance
+  void *d_fft_list = nullptr;
   // device tables
   void *d_desc = nullptr, *d_count_items = nullptr, *d_tile_series = nullptr, *d_col_items = nullptr,
        *d_row_items = nullptr, *d_small_list = nullptr;
@@ -217,7 +278,7 @@ struct cuna2_batch_plan_st {
   size_t desc_bytes = 0;
   // workspace
   void *ws = nullptr;
-  int *counts = nullptr, *offsets = nullptr, *cursor = nullptr;
+  int *counts = nullptr, *offsets = nullptr, *cursor = nullptr, *scan_totals = nullptr;
   void *recs = nullptr, *grid = nullptr;
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -244,6 +305,7 @@ template <typename T> int batch_build(cuna2_batch_plan_st *p) {
   std::vector<Item> count_items, col_items, row_items;
   std::vector<int> tile_series;
   std::map<int, std::vector<int>> small;  // logL -> series
+  std::map<int, std::vector<int>> large;  // logL -> series
   int64_t s_off = 0, f_off = 0, g_off = 0;
   int tile0 = 0;
   for (int s = 0; s < p->nseries; ++s) {
@@ -281,6 +343,7 @@ template <typename T> int batch_build(cuna2_batch_plan_st *p) {
       for (int pb = 0; pb < (npairs + PB - 1) / PB; ++pb) row_items.push_back({s, pb, 0, 0});
       p->smem_col = std::max(p->smem_col, sizeof(C) * (size_t)BA * fft_pitch(L1, BA));
       p->smem_row = std::max(p->smem_row, sizeof(C) * (size_t)BB * fft_pitch(L2, BB));
+      large[logL].push_back(s);
       tile0 += d.ntiles;
       g_off += ng;
       p->large_samples += d.n;
@@ -302,6 +365,16 @@ template <typename T> int batch_build(cuna2_batch_plan_st *p) {
     p->small_class_off.push_back((int)small_list.size());
     small_list.insert(small_list.end(), kv.second.begin(), kv.second.end());
   }
+  std::vector<int> fft_list;
+  p->fft_ct = true;
+  const int lo = dbl ? 14 : 15, hi = dbl ? 23 : 25;
+  for (auto &kv : large) {
+    p->fft_classes.push_back({kv.first, (int)kv.second.size()});
+    p->fft_class_off.push_back((int)fft_list.size());
+    fft_list.insert(fft_list.end(), kv.second.begin(), kv.second.end());
+    if (kv.first < lo || kv.first > hi || kv.second.size() > 65535) p->fft_ct = false;
+  }
+  CUNA_TRY(upload(fft_list, &p->d_fft_list));
   p->desc_bytes = sizeof(BDesc<T>) * desc.size();
   p->host_desc = malloc(p->desc_bytes ? p->desc_bytes : 1);
   if (!p->host_desc) return fail(CUNA2_ERROR_ALLOC, "host descriptor table");
@@ -312,10 +385,11 @@ template <typename T> int batch_build(cuna2_batch_plan_st *p) {
   CUNA_TRY(upload(col_items, &p->d_col_items));
   CUNA_TRY(upload(row_items, &p->d_row_items));
   CUNA_TRY(upload(small_list, &p->d_small_list));
-  // workspace: counts | offsets | cursor | records | grid
+  // workspace: counts | offsets | cursor | scan totals | records | grid
   const size_t nt = (size_t)std::max(1, p->tiles_total);
   const size_t o_off = align_up(sizeof(int) * nt), o_cur = o_off + align_up(sizeof(int) * (nt + 1));
-  const size_t o_rec = o_cur + align_up(sizeof(int) * nt);
+  const size_t o_tot = o_cur + align_up(sizeof(int) * nt);
+  const size_t o_rec = o_tot + align_up(sizeof(int) * (nt / kScanChunk + 1));
   const size_t o_grid = o_rec + align_up(sizeof(Rec) * 2 * (size_t)std::max<int64_t>(1, p->large_samples));
   const size_t bytes = o_grid + sizeof(T) * (size_t)std::max<int64_t>(1, p->grid_total);
   cudaError_t e = cudaMalloc(&p->ws, bytes);
@@ -324,6 +398,7 @@ template <typename T> int batch_build(cuna2_batch_plan_st *p) {
   p->counts = (int *)w;
   p->offsets = (int *)(w + o_off);
   p->cursor = (int *)(w + o_cur);
+  p->scan_totals = (int *)(w + o_tot);
   p->recs = w + o_rec;
   p->grid = w + o_grid;
   CUNA_CK(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
@@ -367,7 +442,15 @@ int batch_run(cuna2_batch_plan_st *p, const double *t, const T *y, typename CxOf
       k_bcount<T><<<p->n_count_items, 512, p->smem_bin / 2, st>>>(t, y, D, (const Item *)p->d_count_items, p->counts);
       CUNA_CK(cudaGetLastError());
     }
-    k_scan_tiles<<<1, 1024, 0, st>>>(p->counts, p->offsets, p->cursor, ntl);
+    if (ntl <= 2 * kScanChunk) {
+      k_scan_tiles<<<1, 1024, 0, st>>>(p->counts, p->offsets, p->cursor, ntl);
+    } else {
+      const int nb = (ntl + kScanChunk - 1) / kScanChunk;
+      int *totals = p->scan_totals;
+      k_scan_blocks<<<nb, 1024, 0, st>>>(p->counts, p->offsets, totals, ntl);
+      CUNA_CK(cudaGetLastError());
+      k_scan_add<<<nb, 1024, 0, st>>>(p->offsets, totals, p->cursor, ntl, nb);
+    }
     CUNA_CK(cudaGetLastError());
     if (p->n_count_items > 0) {
       k_bscatter<T><<<p->n_count_items, 512, p->smem_bin, st>>>(t, y, D, (const Item *)p->d_count_items, p->offsets,
@@ -378,11 +461,20 @@ int batch_run(cuna2_batch_plan_st *p, const double *t, const T *y, typename CxOf
     k_bgrid<T><<<ntl, kGridThreads, smg, st>>>((const Rec *)p->recs, p->offsets, (T *)p->grid, D,
                                                (const int *)p->d_tile_series);
     CUNA_CK(cudaGetLastError());
-    const int threads = (sizeof(T) == 4 ? kPassElemsF32 : kPassElemsF64) / kFftE;
-    k_bcolpass<T><<<p->n_col_items, threads, p->smem_col, st>>>((T *)p->grid, D, (const Item *)p->d_col_items);
-    CUNA_CK(cudaGetLastError());
-    k_browpass<T><<<p->n_row_items, threads, p->smem_row, st>>>((const T *)p->grid, D, (const Item *)p->d_row_items, F);
-    CUNA_CK(cudaGetLastError());
+    if (p->fft_ct) {  // one column and one row launch per size class
+      for (size_t c = 0; c < p->fft_classes.size(); ++c) {
+        const int r = bct_passes<T>(p->fft_classes[c].first, (T *)p->grid, D,
+                                    (const int *)p->d_fft_list + p->fft_class_off[c], p->fft_classes[c].second, F, st);
+        if (r != 1) return fail_cuda(cudaGetLastError(), "batched FFT pass launch");
+      }
+    } else {
+      const int threads = (sizeof(T) == 4 ? kPassElemsF32 : kPassElemsF64) / kFftE;
+      k_bcolpass<T><<<p->n_col_items, threads, p->smem_col, st>>>((T *)p->grid, D, (const Item *)p->d_col_items);
+      CUNA_CK(cudaGetLastError());
+      k_browpass<T><<<p->n_row_items, threads, p->smem_row, st>>>((const T *)p->grid, D, (const Item *)p->d_row_items,
+                                                                  F);
+      CUNA_CK(cudaGetLastError());
+    }
   }
   if (!p->small_classes.empty()) CUNA_CK(cudaStreamWaitEvent(st, p->ev_join, 0));
   return CUNA2_SUCCESS;
@@ -427,6 +519,7 @@ void batch_free(cuna2_batch_plan_st *p) {
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_join) cudaEventDestroy(p->ev_join);
   for (void *d : {p->d_desc, p->d_count_items, p->d_tile_series, p->d_col_items, p->d_row_items, p->d_small_list,
+                  p->d_fft_list,
                   p->ws})
     if (d) cudaFree(d);
   free(p->host_desc);

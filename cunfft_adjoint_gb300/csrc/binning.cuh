@@ -263,6 +263,40 @@ __global__ void __launch_bounds__(512) k_bin_scan_scatter(S smp, const int *__re
     for (int q = 0; q < p[it].nt; ++q) recs[lbase[p[it].t[q]] + rk[it][q]] = p[it].rec;
 }
 
+// Multi-CTA form of k_scan_tiles for long tile lists: k_scan_blocks scans
+// chunks of kScanChunk counts per CTA (local exclusive offsets + chunk
+// totals), k_scan_add adds each chunk's prefix of totals, writes
+// offsets[ntiles] and zeroes cursor.
+constexpr int kScanChunk = 4096;  // 1024 threads x 4
+
+__global__ void __launch_bounds__(1024) k_scan_blocks(const int *__restrict__ counts, int *__restrict__ offsets,
+                                                      int *__restrict__ totals, int ntiles) {
+  __shared__ int in[kScanChunk], out[kScanChunk + 1];
+  const int base = blockIdx.x * kScanChunk, cnt = min(kScanChunk, ntiles - base);
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) in[i] = counts[base + i];
+  __syncthreads();
+  cta_exclusive_scan(in, out, cnt);
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) offsets[base + i] = out[i];
+  if (threadIdx.x == 0) totals[blockIdx.x] = out[cnt];
+}
+
+__global__ void __launch_bounds__(1024) k_scan_add(int *__restrict__ offsets, const int *__restrict__ totals,
+                                                   int *__restrict__ cursor, int ntiles, int nblocks) {
+  __shared__ int add;
+  if (threadIdx.x == 0) {
+    int a = 0;
+    for (int b = 0; b < (int)blockIdx.x; ++b) a += totals[b];
+    add = a;
+    if (blockIdx.x == nblocks - 1) offsets[ntiles] = a + totals[blockIdx.x];
+  }
+  __syncthreads();
+  const int base = blockIdx.x * kScanChunk, cnt = min(kScanChunk, ntiles - base);
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+    offsets[base + i] += add;
+    cursor[base + i] = 0;
+  }
+}
+
 // k_bin_local: single-pass binning into chunk-local tile order.  CTA c takes
 // the samples [c CH, (c+1) CH), counts its records per tile in shared memory,
 // scans the counts, and writes its records tile by tile into its own region

@@ -169,9 +169,9 @@ template <int LOGN> __host__ __device__ constexpr int last_logns() {
   return LOGN <= 4 ? 0 : LOGN - 4;
 }
 
+// column block `cblock` of one packed grid z (L1 x L2 complex, row-major)
 template <typename T, int LOGL>
-__global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_colpass(typename CxOf<T>::type *grid, FftDev<T> f,
-                                                                    int64_t slab_stride) {
+__device__ __forceinline__ void ct_colpass_body(typename CxOf<T>::type *z, const FftDev<T> &f, int cblock) {
   typedef typename CxOf<T>::type C;
   constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
   constexpr int LOGB = ilog2c(PassCfg<T>::ELEMS) - LOG1;
@@ -181,8 +181,8 @@ __global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_colpass(typename CxO
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *s = reinterpret_cast<C *>(smem_raw);
   C *steps = s + PITCH * B;
-  const int c0 = blockIdx.x * B;
-  C *slab = grid + blockIdx.y * slab_stride + c0;
+  const int c0 = cblock * B;
+  C *slab = z + c0;
   // stride 17 so that the columns of one row of the table fall in different banks
   for (int i = threadIdx.x; i < 16 * B; i += PassCfg<T>::THREADS)
     steps[(i >> 4) * 17 + (i & 15)] = twiddle_L(f, (c0 + (i >> 4)) * ((i & 15) << LNS));
@@ -191,6 +191,12 @@ __global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_colpass(typename CxO
   CtColDst<T, LOG1, LOG2, LOGB> dst{slab, steps, f, c0};
   // reads all precede the first barrier, writes all follow it: in place is safe
   ct_fft<T, LOG1, LOGB, true, true, true>(s, f.tw1, src, dst);
+}
+
+template <typename T, int LOGL>
+__global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_colpass(typename CxOf<T>::type *grid, FftDev<T> f,
+                                                                    int64_t slab_stride) {
+  ct_colpass_body<T, LOGL>(grid + blockIdx.y * slab_stride, f, blockIdx.x);
 }
 
 template <typename T, int LOGL> constexpr size_t ct_colpass_smem() {
@@ -219,10 +225,10 @@ struct CtNoDst {
   template <int R, int LOGNS, typename C> __device__ void store(int, int, C *) const {}
 };
 
+// row-pair block `pblock` of one packed grid z; outputs Fs[0 .. nf)
 template <typename T, int LOGL>
-__global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_rowpass_acc(const typename CxOf<T>::type *__restrict__ grid,
-                                                                        FftDev<T> f, AccParams<T> e,
-                                                                        typename CxOf<T>::type *F) {
+__device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *__restrict__ slab, const FftDev<T> &f,
+                                                const AccParams<T> &e, typename CxOf<T>::type *Fs, int pblock) {
   typedef typename CxOf<T>::type C;
   constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
   constexpr int L1 = 1 << LOG1, L2 = 1 << LOG2;
@@ -232,9 +238,7 @@ __global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_rowpass_acc(const ty
   constexpr int THREADS = PassCfg<T>::THREADS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *s = reinterpret_cast<C *>(smem_raw);
-  const int p0 = blockIdx.x * P;
-  const C *slab = grid + ((int64_t)blockIdx.y << LOGL);
-  C *Fs = F + (int64_t)blockIdx.y * e.nf;
+  const int p0 = pblock * P;
   CtPairSrc<T, LOG1, LOG2> src{slab, p0};
   ct_fft<T, LOG2, LOGB, false, false, false>(s, f.tw2, src, CtNoDst());
   constexpr int npairs = L1 / 2 + 1;
@@ -253,6 +257,13 @@ __global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_rowpass_acc(const ty
     const C Zm = cconj(s[(2 * i + 1 - half) * PITCH + cpad16(k2m)]);
     acc_output<T>(e, k, Zk, Zm, Fs);
   }
+}
+
+template <typename T, int LOGL>
+__global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_rowpass_acc(const typename CxOf<T>::type *__restrict__ grid,
+                                                                        FftDev<T> f, AccParams<T> e,
+                                                                        typename CxOf<T>::type *F) {
+  ct_rowpass_body<T, LOGL>(grid + ((int64_t)blockIdx.y << LOGL), f, e, F + (int64_t)blockIdx.y * e.nf, blockIdx.x);
 }
 
 template <typename T, int LOGL> constexpr size_t ct_rowpass_smem() {

@@ -81,3 +81,22 @@ def test_uneven_batch_matches_single_plans(nfft):
         Si = single(torch.as_tensor(ts[i], device="cuda"), torch.as_tensor(ys[i], device="cuda"), 0.0, T[i])
         torch.cuda.synchronize()
         assert rel_l2(Fi.cpu().numpy(), Si.cpu().numpy()) < 1e-6, i
+
+
+def test_large_batch_multi_block_scan_and_classes(nfft, oracle_lib):
+    """A batch whose large series need more than 8192 tiles (the multi-CTA
+    tile scan) spread over four FFT size classes, against the NDFT."""
+    rng = np.random.default_rng(23)
+    nser = 200
+    nf = np.array([1 << int(v) for v in rng.integers(15, 19, nser)], dtype=np.int64)
+    n = rng.integers(500, 3000, nser).astype(np.int64)
+    T = np.exp(rng.uniform(np.log(10), np.log(3000), nser))
+    ts = [rng.uniform(0, T[i], n[i]) for i in range(nser)]
+    ys = [rng.normal(0, 1, n[i]).astype(np.float32) for i in range(nser)]
+    plan = nfft.BatchAdjointNFFT(n, nf, 2, 8, np.zeros(nser), T, torch.float32)
+    F = plan(torch.as_tensor(np.concatenate(ts), device="cuda"), torch.as_tensor(np.concatenate(ys), device="cuda"))
+    parts = plan.split(F)
+    for i in rng.choice(nser, 8, replace=False):
+        k = np.sort(rng.choice(np.arange(-nf[i] // 2, nf[i] // 2), 64, replace=False))
+        D = oracle_lib.ndft(ts[i], ys[i].astype(np.float64), 0.0, T[i], k)
+        assert rel_l2(parts[i].cpu().numpy()[k + nf[i] // 2], D) < 1e-5, i
