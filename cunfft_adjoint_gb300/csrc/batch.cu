@@ -112,13 +112,13 @@ __global__ void __launch_bounds__(512) k_bscatter(const double *__restrict__ t, 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 4 : 2) k_bgrid(
+__global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 2) k_bgrid(
     const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
     const BDesc<T> *__restrict__ D, const int *__restrict__ tile_series) {
   const int gt = blockIdx.x;
   const BDesc<T> d = D[tile_series[gt]];
-  grid_tile_body<T, 4>(recs, off[gt], off[gt + 1], (gt - d.tile0) << d.e.logTL, grid + d.g_off, d.e, nullptr, 0, 0, 1,
-                    0);
+  grid_tile_fixed<T>(recs, off[gt], off[gt + 1], (gt - d.tile0) << d.e.logTL, grid + d.g_off, d.e, nullptr, 0, 0,
+                     1, 0);
 }
 
 template <typename T>
@@ -457,7 +457,7 @@ int batch_run(cuna2_batch_plan_st *p, const double *t, const T *y, typename CxOf
                                                                p->cursor, (Rec *)p->recs);
       CUNA_CK(cudaGetLastError());
     }
-    const size_t smg = grid_smem_bytes<T>(12, p->m);
+    const size_t smg = grid_fixed_smem_bytes<T>(12, p->m);
     k_bgrid<T><<<ntl, kGridThreads, smg, st>>>((const Rec *)p->recs, p->offsets, (T *)p->grid, D,
                                                (const int *)p->d_tile_series);
     CUNA_CK(cudaGetLastError());
