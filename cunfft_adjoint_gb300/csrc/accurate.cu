@@ -189,8 +189,9 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   const int nslab = multi ? nmulti : (nbs > 0 ? nbs : 1);
   const PhaseMul pm = phase_setup(t0, T_);
   const AccParams<T> e = make_params<T>(p);
-  // one transform of a small plan runs tiled over many CTAs when it can
-  const bool small = p->small && !(p->has_split && p->tiled_single && nslab == 1);
+  // a few slabs of a small plan (one transform, a few channels) run tiled
+  // over many CTAs when they can; many slabs take one CTA each
+  const bool small = p->small && !(p->has_split && p->tiled_single && 2 * nslab <= device_sm_count());
   const FftDev<T> f = to_dev<T>(small || !p->small ? p->geom : p->geom4);
   const int L = 1 << p->geom.logL;
   const int ntiles = p->ntiles;
