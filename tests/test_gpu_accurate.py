@@ -271,3 +271,23 @@ def test_host_async_two_streams(nfft):
     for s in range(4):
         ref = plans[0](torch.as_tensor(ts[s], device="cuda"), torch.as_tensor(ys[s], device="cuda"), 0.0, T)
         assert rel_l2(Fh[s].numpy(), ref.cpu().numpy()) < 1e-6
+
+
+@pytest.mark.parametrize("dtype,nf,R,tol", [(torch.float32, 1 << 24, 4, 1e-5), (torch.float64, 1 << 22, 4, 1e-9)])
+def test_largest_plans(nfft, oracle_lib, dtype, nf, R, tol):
+    """The largest grids a plan accepts (2^25 packed points float, 2^23
+    double) against the NDFT on 64 bins; one point more is refused."""
+    rng = np.random.default_rng(5)
+    n, T = 300_000, 1000.0
+    t = rng.uniform(0, T, n)
+    y = rng.normal(0, 1, n)
+    plan = nfft.AdjointNFFT(nf, R, 12, dtype)
+    F = plan(torch.as_tensor(t, device="cuda"), torch.as_tensor(y, dtype=dtype, device="cuda"), 0.0, T)
+    k = np.sort(rng.choice(np.arange(-nf // 2, nf // 2), 64, replace=False))
+    D = oracle_lib.ndft(t, y, 0.0, T, k)
+    assert rel_l2(F.cpu().numpy()[k + nf // 2], D) < tol
+    del F, plan
+    torch.cuda.empty_cache()
+    from cunfft_adjoint_gb300 import _lib
+    with pytest.raises(_lib.CunaError):
+        nfft.AdjointNFFT(2 * nf, R, 12, dtype)

@@ -100,3 +100,24 @@ def test_large_batch_multi_block_scan_and_classes(nfft, oracle_lib):
         k = np.sort(rng.choice(np.arange(-nf[i] // 2, nf[i] // 2), 64, replace=False))
         D = oracle_lib.ndft(ts[i], ys[i].astype(np.float64), 0.0, T[i], k)
         assert rel_l2(parts[i].cpu().numpy()[k + nf[i] // 2], D) < 1e-5, i
+
+
+def test_batch_with_empty_and_tiny_series(nfft, oracle_lib):
+    """Series of 0, 1 and 2 samples (small and large grids) inside a batch:
+    empty series give zero spectra, the others the NDFT."""
+    rng = np.random.default_rng(31)
+    n = np.array([0, 1, 2, 5000, 0, 1, 30000, 3], dtype=np.int64)
+    nf = np.array([1024, 4096, 1 << 16, 1 << 14, 1 << 17, 1 << 16, 1 << 17, 256], dtype=np.int64)
+    T = rng.uniform(10, 100, len(n))
+    ts = [rng.uniform(0, T[i], n[i]) for i in range(len(n))]
+    ys = [rng.normal(0, 1, n[i]).astype(np.float32) for i in range(len(n))]
+    plan = nfft.BatchAdjointNFFT(n, nf, 2, 8, np.zeros(len(n)), T, torch.float32)
+    F = plan(torch.as_tensor(np.concatenate(ts), device="cuda"), torch.as_tensor(np.concatenate(ys), device="cuda"))
+    parts = [p.cpu().numpy() for p in plan.split(F)]
+    for i in range(len(n)):
+        if n[i] == 0:
+            assert not np.any(parts[i]), i
+            continue
+        k = np.arange(-nf[i] // 2, nf[i] // 2)[:: max(1, nf[i] // 256)]
+        D = oracle_lib.ndft(ts[i], ys[i].astype(np.float64), 0.0, T[i], k)
+        assert rel_l2(parts[i][k + nf[i] // 2], D) < 1e-5, i
