@@ -75,6 +75,7 @@ CORE_SIGNATURES = {
     "cuna2_plan_set_graph": (_I, [_P, _I]),
     "cuna2_plan_set_schedule": (_I, [_P, _I, _I]),
     "cuna2_plan_set_binning": (_I, [_P, _I]),
+    "cuna2_plan_create_auto": (_I, [_P, _I, _I64, _D, _P, _P, _P, _I64, _D, _D, _P, _P, _P]),
     "cuna2_plan_get_binning": (_I, [_P, _P]),
     "cuna2_plan_get_schedule": (_I, [_P, _P, _P]),
     "cuna2_plan_autotune": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P, _I, _P]),

@@ -731,6 +731,54 @@ extern "C" int cuna2_plan_autotune(cuna2_plan p, const double *t, const void *y,
   return CUNA2_SUCCESS;
 }
 
+// Filter-width schedule: the candidate (R, m) pairs for an error target and
+// a choice among them by timing on the caller's data.
+extern "C" int cuna2_plan_create_auto(cuna2_plan *plan, int dtype, int64_t nf, double tol, const double *t,
+                                      const void *y, void *F, int64_t n, double t0, double T, cudaStream_t st,
+                                      int *R_out, int *m_out) {
+  clear_error();
+  if (!plan || !F || !(tol > 0) || !(tol < 1)) return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
+  *plan = nullptr;
+  // the Gaussian kernel's error is about exp(-pi m sqrt(1 - 1/R)); float
+  // plans cannot go below their rounding, so the target is clamped there
+  const double target = std::max(tol, dtype == CUNA2_F32 ? 1e-7 : 1e-15);
+  cuna2_plan best = nullptr;
+  float best_ms = 3.4e38f;
+  int bR = 0, bm = 0;
+  for (int R = 2; R <= 8; R *= 2) {
+    int m = (int)std::ceil(-std::log(target) / (kPi * std::sqrt(1.0 - 1.0 / R)));
+    m = std::max(m, 2);
+    if (m > 16) continue;
+    cuna2_plan c = nullptr;
+    if (cuna2_plan_create(&c, dtype, nf, R, m) != CUNA2_SUCCESS) {
+      clear_error();
+      continue;
+    }
+    float ms = 0;
+    const int s = cuna2_plan_autotune(c, t, y, F, n, t0, T, st, 3, &ms);
+    if (s != CUNA2_SUCCESS) {
+      cuna2_plan_destroy(c);
+      if (best) cuna2_plan_destroy(best);
+      return s;
+    }
+    if (ms < best_ms) {
+      if (best) cuna2_plan_destroy(best);
+      best = c;
+      best_ms = ms;
+      bR = R;
+      bm = m;
+    } else {
+      cuna2_plan_destroy(c);
+    }
+  }
+  if (!best) return fail(CUNA2_ERROR_UNSUPPORTED, "no plan for nf=%lld reaches tol=%g with m <= 16", (long long)nf, tol);
+  clear_error();
+  *plan = best;
+  if (R_out) *R_out = bR;
+  if (m_out) *m_out = bm;
+  return CUNA2_SUCCESS;
+}
+
 extern "C" int cuna2_plan_set_binning(cuna2_plan p, int mode) {
   clear_error();
   if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");

@@ -15,6 +15,30 @@ from . import _lib
 
 
 class AdjointNFFT:
+    @classmethod
+    def for_tolerance(cls, nf, tol, t, y, t0=None, T=None, dtype=torch.float32):
+        """The plan (R, m, schedule) that reaches relative error `tol` fastest
+        on the representative input (t, y) (cuna2_plan_create_auto)."""
+        self = cls.__new__(cls)
+        self.nf, self.dtype = int(nf), dtype
+        self.device = t.device
+        self.cdtype = torch.complex64 if dtype == torch.float32 else torch.complex128
+        self._h = ctypes.c_void_p()
+        t, y, t0, T = AdjointNFFT._check(self, t, y, t0, T)
+        out = torch.empty(self.nf, dtype=self.cdtype, device=t.device)
+        R, m = ctypes.c_int(), ctypes.c_int()
+        s = torch.cuda.current_stream(t.device).cuda_stream
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.core().cuna2_plan_create_auto(
+                ctypes.byref(self._h), _lib.F32 if dtype == torch.float32 else _lib.F64, self.nf, float(tol),
+                t.data_ptr(), y.data_ptr(), out.data_ptr(), t.numel(), float(t0), float(T), s or None,
+                ctypes.byref(R), ctypes.byref(m)))
+        self.R, self.m = R.value, m.value
+        ng, tau = ctypes.c_int64(), ctypes.c_double()
+        _lib.check(_lib.core().cuna2_plan_info(self._h, ctypes.byref(ng), ctypes.byref(tau)))
+        self.ng, self.tau = ng.value, tau.value
+        return self
+
     def __init__(self, nf, R=2, m=8, dtype=torch.float32, device=None):
         if dtype not in (torch.float32, torch.float64):
             raise TypeError("dtype must be torch.float32 or torch.float64")

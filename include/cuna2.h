@@ -261,6 +261,17 @@ enum { CUNA2_GRID_GATHER = 0, CUNA2_GRID_SCATTER = 1, CUNA2_GRID_FIXED = 2 };
 int cuna2_plan_set_schedule(cuna2_plan plan, int log_tile, int grid_method);
 int cuna2_plan_get_schedule(cuna2_plan plan, int *log_tile, int *grid_method);
 
+/* Filter-width schedule: creates the plan for nf outputs that reaches a
+ * relative error target `tol` fastest on the caller's data.  For each
+ * oversampling R in {2, 4, 8} it takes the smallest half-width m with
+ * exp(-pi m sqrt(1 - 1/R)) <= tol (the Gaussian kernel's error; clamped at
+ * 1e-7 for float plans), autotunes that plan on (t, y) (writing F, nf
+ * values) and keeps the fastest; R_out / m_out (may be NULL) receive the
+ * choice.  The reference fixes its filter width (R_f 6 / 12). */
+int cuna2_plan_create_auto(cuna2_plan *plan, int dtype, int64_t nf, double tol, const double *t,
+                           const void *y, void *F, int64_t n, double t0, double T, cudaStream_t stream,
+                           int *R_out, int *m_out);
+
 /* Bucket sort in front of the tiled gridding:
  *   CUNA2_BIN_GLOBAL  count pass, then one pass that scans the tile counts and
  *                     scatters the records into one tile-ordered array;

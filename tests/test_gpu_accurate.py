@@ -291,3 +291,22 @@ def test_largest_plans(nfft, oracle_lib, dtype, nf, R, tol):
     from cunfft_adjoint_gb300 import _lib
     with pytest.raises(_lib.CunaError):
         nfft.AdjointNFFT(2 * nf, R, 12, dtype)
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-5), (torch.float64, 1e-9)])
+def test_plan_for_tolerance(nfft, oracle_lib, dtype, tol):
+    """The filter-width chooser returns a plan whose kernel error estimate
+    meets the target and whose spectrum meets it against the NDFT."""
+    rng = np.random.default_rng(8)
+    n, nf, T = 100_000, 1 << 16, 200.0
+    t = rng.uniform(0, T, n)
+    y = rng.normal(0, 1, n)
+    td = torch.as_tensor(t, device="cuda")
+    yd = torch.as_tensor(y, dtype=dtype, device="cuda")
+    plan = nfft.AdjointNFFT.for_tolerance(nf, tol, td, yd, 0.0, T, dtype)
+    assert plan.R in (2, 4, 8) and 2 <= plan.m <= 16
+    assert np.exp(-np.pi * plan.m * np.sqrt(1 - 1 / plan.R)) <= max(tol, 1e-7)
+    F = plan(td, yd, 0.0, T).cpu().numpy()
+    k = np.sort(rng.choice(np.arange(-nf // 2, nf // 2), 128, replace=False))
+    D = oracle_lib.ndft(t, y, 0.0, T, k)
+    assert rel_l2(F[k + nf // 2], D) < tol
