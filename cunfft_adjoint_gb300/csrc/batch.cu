@@ -148,7 +148,8 @@ __global__ void __launch_bounds__(PassCfg<T>::THREADS) k_bct_colpass(T *grid, co
                                                                      const int *__restrict__ list) {
   typedef typename CxOf<T>::type C;
   const int s = list[blockIdx.y];
-  ct_colpass_body<T, LOGL>(reinterpret_cast<C *>(grid + D[s].g_off), D[s].f, blockIdx.x);
+  C *z = reinterpret_cast<C *>(grid + D[s].g_off);
+  ct_colpass_body<T, LOGL>(z, z, D[s].f, blockIdx.x);
 }
 
 template <typename T, int LOGL>

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include "binning.cuh"
 #include "fft.cuh"
+#include "fftpass_core.cuh"
 #include "rng.cuh"
 #include "runtime.h"
 
@@ -266,6 +267,92 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_fft_rowpass_comp
   fft_fused<T, true, false, true>(s, pitch, f.logL2, logB, f.tw2, src, dst);
 }
 
+// Compile-time four-step passes of the compat transform: column pass from
+// f_hat into scratch (twiddled), row pass from scratch back into f_hat in
+// natural order with the reference normalisation fused in.
+template <typename T, int LOGL>
+__global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_colpass_oop(const typename CxOf<T>::type *in,
+                                                                        typename CxOf<T>::type *out, FftDev<T> f,
+                                                                        int64_t slab_stride) {
+  ct_colpass_body<T, LOGL>(in + blockIdx.y * slab_stride, out + blockIdx.y * slab_stride, f, blockIdx.x);
+}
+
+template <typename T, int LOG2> struct CtRowSrc {
+  const typename CxOf<T>::type *p;  // first row of the block
+  __device__ __forceinline__ typename CxOf<T>::type load(int seq, int j, int dr) const {
+    return p[(seq << LOG2) + j + dr];
+  }
+};
+
+template <typename T, int LOG1> struct CtFacDst {
+  typename CxOf<T>::type *p;  // slab
+  int ng, r0, norm;
+  T b, nf;
+  template <int R, int LOGNS>
+  __device__ __forceinline__ void store(int seq, int idxD, typename CxOf<T>::type *v) const {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int k = r0 + seq + ((idxD + (r << LOGNS)) << LOG1);
+      p[k] = norm ? cscale(v[r], compat_fac(k, ng, b, nf)) : v[r];
+    }
+  }
+};
+
+template <typename T, int LOGL>
+__global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_rowpass_compat(const typename CxOf<T>::type *in,
+                                                                           typename CxOf<T>::type *out, FftDev<T> f,
+                                                                           const typename FpOf<T>::type *fp,
+                                                                           int64_t slab_stride, int norm) {
+  typedef typename CxOf<T>::type C;
+  constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
+  constexpr int LOGB = ilog2c(PassCfg<T>::ELEMS) - LOG2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *s = reinterpret_cast<C *>(smem_raw);
+  const int r0 = blockIdx.x << LOGB;
+  CtRowSrc<T, LOG2> src{in + blockIdx.y * slab_stride + ((int64_t)r0 << LOG2)};
+  CtFacDst<T, LOG1> dst{out + blockIdx.y * slab_stride, 1 << LOGL, r0, norm, fp->b, fp->normfac};
+  // rows are read point-fastest (contiguous), outputs written row-fastest
+  ct_fft<T, LOG2, LOGB, true, false, true>(s, f.tw2, src, dst);
+}
+
+template <typename T, int LOGL>
+int compat_ct_at(typename CxOf<T>::type *f_hat, typename CxOf<T>::type *scratch, const FftDev<T> &f,
+                 const typename FpOf<T>::type *dfp, int nbs, bool norm, cudaStream_t st) {
+  constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
+  constexpr int BA = PassCfg<T>::ELEMS >> LOG1, BB = PassCfg<T>::ELEMS >> LOG2;
+  constexpr size_t smA = ct_colpass_smem<T, LOGL>();
+  constexpr size_t smB = sizeof(typename CxOf<T>::type) * (size_t)fft_pitch(1 << LOG2, BB) * BB;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(k_ct_colpass_oop<T, LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smA) ||
+        cudaFuncSetAttribute(k_ct_rowpass_compat<T, LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smB))
+      return -1;
+    attr = true;
+  }
+  const int64_t L = (int64_t)1 << LOGL;
+  k_ct_colpass_oop<T, LOGL><<<dim3((1 << LOG2) / BA, nbs), PassCfg<T>::THREADS, smA, st>>>(f_hat, scratch, f, L);
+  if (cudaPeekAtLastError() != cudaSuccess) return -1;
+  k_ct_rowpass_compat<T, LOGL><<<dim3((1 << LOG1) / BB, nbs), PassCfg<T>::THREADS, smB, st>>>(scratch, f_hat, f, dfp,
+                                                                                            L, norm ? 1 : 0);
+  if (cudaPeekAtLastError() != cudaSuccess) return -1;
+  return 1;
+}
+
+// 1: launched, 0: no compiled instance, -1: launch error
+template <typename T>
+int compat_ct(int logL, typename CxOf<T>::type *f_hat, typename CxOf<T>::type *scratch, const FftDev<T> &f,
+              const typename FpOf<T>::type *dfp, int nbs, bool norm, cudaStream_t st) {
+#define CUNA_CCT(LG) \
+  case LG: return compat_ct_at<T, LG>(f_hat, scratch, f, dfp, nbs, norm, st);
+  if constexpr (sizeof(T) == 4) {
+    switch (logL) { CUNA_CCT(15) CUNA_CCT(16) CUNA_CCT(17) CUNA_CCT(18) CUNA_CCT(19) CUNA_CCT(20) CUNA_CCT(21) CUNA_CCT(22) CUNA_CCT(23) CUNA_CCT(24) CUNA_CCT(25) }
+  } else {
+    switch (logL) { CUNA_CCT(14) CUNA_CCT(15) CUNA_CCT(16) CUNA_CCT(17) CUNA_CCT(18) CUNA_CCT(19) CUNA_CCT(20) CUNA_CCT(21) CUNA_CCT(22) CUNA_CCT(23) }
+  }
+#undef CUNA_CCT
+  return 0;
+}
+
 template <typename T>
 __global__ void k_compat_normalize(typename CxOf<T>::type *f_hat, int ng, int64_t total,
                                    const typename FpOf<T>::type *fp) {
@@ -367,6 +454,11 @@ int compat_fft(typename CxOf<T>::type *f_hat, int ng, int nbs, const typename Fp
     k_fft_single_compat<T><<<nbs, threads, smem, st>>>(f_hat, f, dfp, norm ? 1 : 0);
     CUNA_CK(cudaGetLastError());
     return CUNA2_SUCCESS;
+  }
+  {
+    const int h = compat_ct<T>(logL, f_hat, scratch, f, dfp, nbs, norm, st);
+    if (h < 0) return fail_cuda(cudaGetLastError(), "FFT pass launch");
+    if (h == 1) return CUNA2_SUCCESS;
   }
   const int elems = sizeof(T) == 4 ? kPassElemsF32 : kPassElemsF64;
   const int threads = elems / kFftE;
