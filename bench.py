@@ -156,7 +156,7 @@ def stage_bytes(n, ng, nf, rec_bytes=16, elem=4):
     }
 
 
-def batched_legs(dev, steps):
+def batched_legs(dev, steps, which=("bootstrap", "uneven"), plain=True):
     """Batched forms: bootstrap (N=5000, 1024 resamples, Nf=32768, R=2, m=8)
     and an uneven batch (4096 series, N log-uniform in [100, 1e5], Nf =
     nextpow2(4N) capped at 2^18, R=2, m=8), float32, CUDA-graph replay.
@@ -167,85 +167,91 @@ def batched_legs(dev, steps):
     rng = np.random.default_rng(3)
     # bootstrap
     n, nbs, nf = 5000, 1024, 32768
-    t = rng.uniform(0, 100.0, n)
-    y = (np.sin(2 * np.pi * t / 2.1) + rng.normal(0, 0.3, n)).astype(np.float32)
-    plan = AdjointNFFT(nf, 2, 8, torch.float32, device=dev)
-    td, yd = torch.as_tensor(t, device=dev), torch.as_tensor(y, device=dev)
-    F = torch.empty((nbs, nf), dtype=torch.complex64, device=dev)
-    for i in range(3):
-        plan.bootstrap(td, yd, nbs, i, 0.0, 100.0, out=F)
-    torch.cuda.synchronize()
-    k = max(3, min(20, steps // 50))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for i in range(k):
-        plan.bootstrap(td, yd, nbs, i, 0.0, 100.0, out=F)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / k
-    out["bootstrap"] = {"workload": "N=5000, 1024 resamples, Nf=32768, R=2, m=8", "value": nbs * 1000.0 / ms,
-                        "unit": UNIT, "ms_per_call": ms, "calls": k}
-    # plain per-resample path: one single-series transform per resample
-    # (resampled inputs prepared outside the timed region)
-    draws = [rng.integers(0, n, n) for _ in range(64)]
-    tds = [td[torch.as_tensor(d, device=dev)] for d in draws]
-    yds = [yd[torch.as_tensor(d, device=dev)] for d in draws]
-    Fp = torch.empty(nf, dtype=torch.complex64, device=dev)
-    for i in range(8):
-        plan.adjoint(tds[i], yds[i], 0.0, 100.0, out=Fp)
-    torch.cuda.synchronize()
-    e0.record()
-    for i in range(len(tds)):
-        plan.adjoint(tds[i], yds[i], 0.0, 100.0, out=Fp)
-    e1.record()
-    torch.cuda.synchronize()
-    msp = e0.elapsed_time(e1) / len(tds)
-    out["bootstrap"]["plain_value"] = 1000.0 / msp
-    out["bootstrap"]["batched_over_plain"] = out["bootstrap"]["value"] / (1000.0 / msp)
-    del F, plan
-    # uneven batch
-    ns = 4096
-    nser = np.exp(rng.uniform(np.log(100), np.log(1e5), ns)).astype(np.int64)
-    nfs = np.minimum(2 ** np.ceil(np.log2(4 * nser)).astype(np.int64), 1 << 18)
-    Ts = np.exp(rng.uniform(np.log(10), np.log(3000), ns))
-    tt = np.concatenate([rng.uniform(0, Ts[i], nser[i]) for i in range(ns)])
-    yy = rng.normal(0, 1, int(nser.sum())).astype(np.float32)
-    bp = BatchAdjointNFFT(nser, nfs, 2, 8, np.zeros(ns), Ts, torch.float32, device=dev, graph=True)
-    tdd, ydd = torch.as_tensor(tt, device=dev), torch.as_tensor(yy, device=dev)
-    FF = torch.empty(int(nfs.sum()), dtype=torch.complex64, device=dev)
-    for i in range(3):
-        bp(tdd, ydd, out=FF)
-    torch.cuda.synchronize()
-    k = max(3, min(10, steps // 100))
-    e0.record()
-    for i in range(k):
-        bp(tdd, ydd, out=FF)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / k
-    out["uneven"] = {"workload": "4096 series, N log-U[100,1e5] (total %d), Nf=nextpow2(4N)<=2^18, R=2, m=8"
-                     % int(nser.sum()), "value": ns * 1000.0 / ms, "unit": UNIT, "ms_per_call": ms, "calls": k}
-    # plain per-series path: one single-series plan call per series (plans
-    # cached per Nf, inputs resident), same series
-    plans = {}
-    offs = np.concatenate([[0], np.cumsum(nser)])
-    foffs = np.concatenate([[0], np.cumsum(nfs)])
-    def plain_all():
-        for i in range(ns):
-            p_ = plans.get(int(nfs[i]))
-            if p_ is None:
-                p_ = plans[int(nfs[i])] = AdjointNFFT(int(nfs[i]), 2, 8, torch.float32, device=dev)
-            p_.adjoint(tdd[offs[i]:offs[i + 1]], ydd[offs[i]:offs[i + 1]], 0.0, float(Ts[i]),
-                       out=FF[foffs[i]:foffs[i + 1]])
-    plain_all()
-    torch.cuda.synchronize()
-    e0.record()
-    plain_all()
-    e1.record()
-    torch.cuda.synchronize()
-    msp = e0.elapsed_time(e1)
-    out["uneven"]["plain_value"] = ns * 1000.0 / msp
-    out["uneven"]["batched_over_plain"] = out["uneven"]["value"] / out["uneven"]["plain_value"]
+    if "bootstrap" in which:
+        t = rng.uniform(0, 100.0, n)
+        y = (np.sin(2 * np.pi * t / 2.1) + rng.normal(0, 0.3, n)).astype(np.float32)
+        plan = AdjointNFFT(nf, 2, 8, torch.float32, device=dev)
+        td, yd = torch.as_tensor(t, device=dev), torch.as_tensor(y, device=dev)
+        F = torch.empty((nbs, nf), dtype=torch.complex64, device=dev)
+        for i in range(3):
+            plan.bootstrap(td, yd, nbs, i, 0.0, 100.0, out=F)
+        torch.cuda.synchronize()
+        k = max(3, min(20, steps // 50))
+        e0.record()
+        for i in range(k):
+            plan.bootstrap(td, yd, nbs, i, 0.0, 100.0, out=F)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        out["bootstrap"] = {"workload": "N=5000, 1024 resamples, Nf=32768, R=2, m=8", "value": nbs * 1000.0 / ms,
+                            "unit": UNIT, "ms_per_call": ms, "calls": k}
+        if plain:
+            # plain per-resample path: one single-series transform per resample
+            # (resampled inputs prepared outside the timed region)
+            draws = [rng.integers(0, n, n) for _ in range(64)]
+            tds = [td[torch.as_tensor(d, device=dev)] for d in draws]
+            yds = [yd[torch.as_tensor(d, device=dev)] for d in draws]
+            Fp = torch.empty(nf, dtype=torch.complex64, device=dev)
+            for i in range(8):
+                plan.adjoint(tds[i], yds[i], 0.0, 100.0, out=Fp)
+            torch.cuda.synchronize()
+            e0.record()
+            for i in range(len(tds)):
+                plan.adjoint(tds[i], yds[i], 0.0, 100.0, out=Fp)
+            e1.record()
+            torch.cuda.synchronize()
+            msp = e0.elapsed_time(e1) / len(tds)
+            out["bootstrap"]["plain_value"] = 1000.0 / msp
+            out["bootstrap"]["batched_over_plain"] = out["bootstrap"]["value"] / (1000.0 / msp)
+        del F, plan
+    if "uneven" in which:
+        # uneven batch (its own seeded stream)
+        rng = np.random.default_rng(4)
+        ns = 4096
+        nser = np.exp(rng.uniform(np.log(100), np.log(1e5), ns)).astype(np.int64)
+        nfs = np.minimum(2 ** np.ceil(np.log2(4 * nser)).astype(np.int64), 1 << 18)
+        Ts = np.exp(rng.uniform(np.log(10), np.log(3000), ns))
+        tt = np.concatenate([rng.uniform(0, Ts[i], nser[i]) for i in range(ns)])
+        yy = rng.normal(0, 1, int(nser.sum())).astype(np.float32)
+        bp = BatchAdjointNFFT(nser, nfs, 2, 8, np.zeros(ns), Ts, torch.float32, device=dev, graph=True)
+        tdd, ydd = torch.as_tensor(tt, device=dev), torch.as_tensor(yy, device=dev)
+        FF = torch.empty(int(nfs.sum()), dtype=torch.complex64, device=dev)
+        for i in range(3):
+            bp(tdd, ydd, out=FF)
+        torch.cuda.synchronize()
+        k = max(3, min(10, steps // 100))
+        e0.record()
+        for i in range(k):
+            bp(tdd, ydd, out=FF)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        out["uneven"] = {"workload": "4096 series, N log-U[100,1e5] (total %d), Nf=nextpow2(4N)<=2^18, R=2, m=8"
+                         % int(nser.sum()), "value": ns * 1000.0 / ms, "unit": UNIT, "ms_per_call": ms, "calls": k}
+        if not plain:
+            return out
+        # plain per-series path: one single-series plan call per series (plans
+        # cached per Nf, inputs resident), same series
+        plans = {}
+        offs = np.concatenate([[0], np.cumsum(nser)])
+        foffs = np.concatenate([[0], np.cumsum(nfs)])
+        def plain_all():
+            for i in range(ns):
+                p_ = plans.get(int(nfs[i]))
+                if p_ is None:
+                    p_ = plans[int(nfs[i])] = AdjointNFFT(int(nfs[i]), 2, 8, torch.float32, device=dev)
+                p_.adjoint(tdd[offs[i]:offs[i + 1]], ydd[offs[i]:offs[i + 1]], 0.0, float(Ts[i]),
+                           out=FF[foffs[i]:foffs[i + 1]])
+        plain_all()
+        torch.cuda.synchronize()
+        e0.record()
+        plain_all()
+        e1.record()
+        torch.cuda.synchronize()
+        msp = e0.elapsed_time(e1)
+        out["uneven"]["plain_value"] = ns * 1000.0 / msp
+        out["uneven"]["batched_over_plain"] = out["uneven"]["value"] / out["uneven"]["plain_value"]
     return out
 
 
@@ -383,11 +389,20 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--streams", type=int, default=3, help="concurrent streams, one plan each")
     ap.add_argument("--no-side-legs", action="store_true", help="skip the float64 and batched legs")
+    ap.add_argument("--only", choices=["bootstrap", "uneven", "autograd"],
+                    help="run one batched leg alone (no plain leg) and print its result")
     ap.add_argument("--nsets", type=int, default=NSETS, help="rotating input sets (default 16: 192 MB > L2)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         return reference_arm(args, wl)
+    if args.only:
+        import torch
+        dev = torch.device("cuda", 0)
+        res = autograd_leg(dev, args.steps) if args.only == "autograd" else \
+            batched_legs(dev, args.steps, (args.only,), plain=False)[args.only]
+        print(json.dumps(res), flush=True)
+        return
 
     import torch
     from cunfft_adjoint_gb300 import _lib
