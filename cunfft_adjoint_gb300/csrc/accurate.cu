@@ -316,6 +316,7 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     const int mx = 200 * 1024;
     CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_acc_sg4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_fixed<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_acc_seg<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
@@ -344,7 +345,10 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
                                                      p->ng);
     }
   } else {
-    if (p->grid_method == CUNA2_GRID_GATHER) {
+    if (p->grid_method == CUNA2_GRID_GATHER && cw8 && wts && group >= 2) {
+      const size_t sm4 = grid_smem_bytes<T>(p->logTL, p->m, 4);
+      k_grid_acc_sg4<T><<<ggrid, gb, sm4, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+    } else if (p->grid_method == CUNA2_GRID_GATHER) {
       if (cw8) k_grid_acc<T, 8><<<ggrid, gb, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
       else k_grid_acc<T, 4><<<ggrid, gb, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
     } else if (p->grid_method == CUNA2_GRID_FIXED) {

@@ -340,7 +340,10 @@ __device__ __forceinline__ void grid_slots(int p0, int ng, int TL, int m, int &s
 // [sbeg, send): slab s grids value wts[s*nvals + p] of sample p when wts is
 // given (bootstrap), else the record's own value.
 // CW consecutive cells per thread in the gather (4 or 8)
-template <typename T, int CW, class Src>
+// SG > 1 (slab weights given, CW = 8 on 2048-cell tiles): SG slabs share each
+// record's Gaussian, computed once per record visit and scaled by each slab's
+// value from shared memory.
+template <typename T, int CW, class Src, int SG = 1>
 __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
                                                int base, T *__restrict__ grid, const AccParams<T> &e,
                                                const T *__restrict__ wts, int64_t nvals, int sbeg, int send,
@@ -357,6 +360,8 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
   int *start = reinterpret_cast<int *>(smem_raw);                                       // W + 1 slots
   SRec<T> *srec = reinterpret_cast<SRec<T> *>(smem_raw + sizeof(int) * ((W + 2 + 3) & ~3));  // placed records
   int *sp = reinterpret_cast<int *>(srec + CAP);                                         // sample index
+  T *yv = reinterpret_cast<T *>(sp + CAP);  // SG > 1: yv[s * CAP + r], value of slab s for placed record r
+  static_assert(SG == 1 || CW == 8, "slab groups run with 8-cell groups on 2048-cell tiles");
   __shared__ int wsum[kGridThreads / 32];
   // a single tile spanning the whole grid maps a record to up to two slots;
   // halve the chunk then so that placements never exceed CAP
@@ -365,10 +370,12 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
   const int nchunks = (r1 - r0 + chunk - 1) / chunk;
   const GaussCW<T, CW> gw(e.k1);
   // the records are sorted once for all slabs when they fit in one chunk
-  for (int slab = sbeg; slab < send; ++slab) {
-    T acc[MAXC];
+  for (int slab = sbeg; slab < send; slab += SG) {
+    T acc[SG][MAXC];
 #pragma unroll
-    for (int q = 0; q < MAXC; ++q) acc[q] = (T)0;
+    for (int g = 0; g < SG; ++g)
+#pragma unroll
+      for (int q = 0; q < MAXC; ++q) acc[g][q] = (T)0;
     for (int ck = 0; ck < nchunks; ++ck) {
       const int c0 = r0 + ck * chunk;
       const int cnt = min(chunk, r1 - c0);
@@ -450,10 +457,20 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
         }
         __syncthreads();
       }
-      if (wts) {  // this slab's values for the placed records
+      if (SG == 1 && wts) {  // this slab's values for the placed records
         const int placed = start[W - 1];
         const T *ws = wts + (int64_t)slab * nvals;
         for (int i = threadIdx.x; i < placed; i += kGridThreads) srec[i].y = ws[sp[i]];
+        __syncthreads();
+      }
+      if constexpr (SG > 1) {  // the group's values (0 past the last slab)
+        const int placed = start[W - 1];
+#pragma unroll
+        for (int g = 0; g < SG; ++g) {
+          const T *ws = wts + (int64_t)(slab + g) * nvals;
+          for (int i = threadIdx.x; i < placed; i += kGridThreads)
+            yv[g * CAP + i] = slab + g < send ? ws[sp[i]] : (T)0;
+        }
         __syncthreads();
       }
       // gather: the thread's cells cl0 .. cl0+CW-1 (local) take the records in
@@ -465,9 +482,10 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
         if (q >= npass || cl0 >= TL) continue;
         const int rb = cl0 == 0 ? 0 : start[cl0 - 1];
         const int re = start[cl0 + CW - 1 + 2 * m - 1];
-        T a[CW];
+        // SG > 1 has one pass (CW = MAXC = 8) and accumulates into acc directly
+        T a[1][CW];
 #pragma unroll
-        for (int i = 0; i < CW; ++i) a[i] = (T)0;
+        for (int i = 0; i < CW; ++i) a[0][i] = (T)0;
         const int ctr = cl0 + m;
         const unsigned w2 = (unsigned)(2 * m);
         for (int r = rb; r < re; ++r) {
@@ -475,28 +493,62 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
           const int rel = rr.lc - cl0;            // lc - c for c = cl0
           const T dd0 = (T)(ctr - rr.lc) - rr.f;  // d - f for c = cl0
           T w[CW];
-          gauss_cw<T, CW>(rr.y, dd0, e.k1, gw, w);
+          gauss_cw<T, CW>(SG > 1 ? (T)1 : rr.y, dd0, e.k1, gw, w);
 #pragma unroll
-          for (int i = 0; i < CW; ++i) a[i] += (unsigned)(rel - i) < w2 ? w[i] : (T)0;
+          for (int i = 0; i < CW; ++i) w[i] = (unsigned)(rel - i) < w2 ? w[i] : (T)0;
+          if constexpr (SG == 1) {
+#pragma unroll
+            for (int i = 0; i < CW; ++i) a[0][i] += w[i];
+          } else {
+#pragma unroll
+            for (int g = 0; g < SG; ++g) {
+              const T yg = yv[g * CAP + r];
+#pragma unroll
+              for (int i = 0; i < CW; ++i) acc[g][i] += yg * w[i];
+            }
+          }
         }
+        if constexpr (SG == 1) {
 #pragma unroll
-        for (int i = 0; i < CW; ++i) acc[CW * q + i] += a[i];
+          for (int i = 0; i < CW; ++i) acc[0][CW * q + i] += a[0][i];
+        }
       }
       __syncthreads();
     }
-    T *out = grid + (int64_t)slab * slab_stride + base;
 #pragma unroll
-    for (int q = 0; q < MAXC / CW; ++q) {
-      const int cl0 = (threadIdx.x + q * kGridThreads) * CW;
-      // TL is a power of two >= CW (gather tiles have >= 512 cells or span the
-      // grid, ng >= 4m >= 4 and CW = 4 there), so groups are whole
-      if (q < npass && cl0 < TL) {
+    for (int g = 0; g < SG; ++g) {
+      if (slab + g >= send) break;
+      T *out = grid + (int64_t)(slab + g) * slab_stride + base;
 #pragma unroll
-        for (int i = 0; i < CW; i += 4)
-          store4(out + cl0 + i, acc[CW * q + i], acc[CW * q + i + 1], acc[CW * q + i + 2], acc[CW * q + i + 3]);
+      for (int q = 0; q < MAXC / CW; ++q) {
+        const int cl0 = (threadIdx.x + q * kGridThreads) * CW;
+        // TL is a power of two >= CW (gather tiles have >= 512 cells or span
+        // the grid, ng >= 4m >= 4 and CW = 4 there), so groups are whole
+        if (q < npass && cl0 < TL) {
+#pragma unroll
+          for (int i = 0; i < CW; i += 4)
+            store4(out + cl0 + i, acc[g][CW * q + i], acc[g][CW * q + i + 1], acc[g][CW * q + i + 2],
+                   acc[g][CW * q + i + 3]);
+        }
       }
     }
   }
+}
+
+// slab groups sharing each record's Gaussian (bootstrap resamples, channels)
+template <typename T>
+__global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 3 : 2) k_grid_acc_sg4(
+    const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
+    AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab, int group, int64_t slab_stride) {
+  const int tile = blockIdx.x;
+  const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
+  const typename RecOf<T>::type *rp = recs;
+  if constexpr (sizeof(T) == 4)
+    grid_tile_body<T, 8, const typename RecOf<T>::type *, 4>(rp, off[tile], off[tile + 1], tile << e.logTL, grid, e,
+                                                              wts, nvals, sbeg, send, slab_stride);
+  else  // double plans keep one slab per pass (four accumulator sets do not fit)
+    grid_tile_body<T, 8>(rp, off[tile], off[tile + 1], tile << e.logTL, grid, e, wts, nvals, sbeg, send,
+                         slab_stride);
 }
 
 template <typename T, int CW>
@@ -846,10 +898,11 @@ template <typename T> size_t grid_scatter_smem_bytes(int logTL) {
   return sizeof(T) * ((size_t)1 << logTL) + (sizeof(SRec<T>) + sizeof(int)) * (size_t)GridCfg<T>::CAP;
 }
 
-template <typename T> size_t grid_smem_bytes(int logTL, int m) {
+template <typename T> size_t grid_smem_bytes(int logTL, int m, int sg = 1) {
   const int W = (1 << logTL) + 2 * m;
   const size_t CAP = GridCfg<T>::CAP;
-  return sizeof(int) * ((W + 2 + 3) & ~3) + sizeof(SRec<T>) * CAP + sizeof(int) * CAP;
+  return sizeof(int) * ((W + 2 + 3) & ~3) + sizeof(SRec<T>) * CAP + sizeof(int) * CAP +
+         (sg > 1 ? sizeof(T) * sg * CAP : 0);
 }
 
 // Last four-step pass of the packed real transform: CTA owns row pairs
