@@ -96,6 +96,24 @@ __device__ __forceinline__ void acc_output(const AccParams<T> &e, int64_t k, typ
   if (k >= 1) F[e.K - k] = cconj(Fk);
 }
 
+// The same with the unpack twiddle exp(2 pi i k / ng) supplied (from tables)
+// and the deconvolution factor by exp2.
+template <typename T>
+__device__ __forceinline__ void acc_output_tw(const AccParams<T> &e, int64_t k, typename CxOf<T>::type Zk,
+                                              typename CxOf<T>::type Zmc, typename CxOf<T>::type *F,
+                                              typename CxOf<T>::type tw) {
+  typedef typename CxOf<T>::type C;
+  const C A = cadd(Zk, Zmc);
+  const C Bv = cmuli(csub(Zmc, Zk));
+  const C G2 = cadd(A, cmul(tw, Bv));
+  const T kf = (T)(int)k;
+  T sc = e.c0 * exp2_t(e.c1 * (T)1.4426950408889634 * kf * kf);
+  if (k & 1) sc = -sc;
+  const C Fk = cscale(G2, sc);
+  if (k < e.K) F[e.K + k] = Fk;
+  if (k >= 1) F[e.K - k] = cconj(Fk);
+}
+
 // ---------------------------------------------------------------------------
 // single-CTA transform for small grids
 // ---------------------------------------------------------------------------

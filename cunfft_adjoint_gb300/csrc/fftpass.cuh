@@ -41,7 +41,22 @@ __device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *__
   constexpr int THREADS = PassCfg<T>::THREADS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *s = reinterpret_cast<C *>(smem_raw);
+  // unpack twiddles W_ng^k = W_ng^{k1} W_ng^{k2 L1} from two small tables
+  // behind the FFT buffer: the CTA's 2P rows and all L2 columns
+  C *twr = s + PITCH * B, *twc = twr + B;
   const int p0 = pblock * P;
+  for (int u = threadIdx.x; u < B + L2; u += THREADS) {
+    int q;
+    if (u < B) {
+      const int pp = p0 + (u >> 1);
+      q = (u & 1) ? ((L1 - pp) & (L1 - 1)) : pp;
+    } else {
+      q = (u - B) << LOG1;
+    }
+    T sn, cs;
+    sincospi_t((T)q * e.twk, &sn, &cs);
+    twr[u] = cmk(cs, sn);  // twr[B + k2] is twc[k2]
+  }
   CtPairSrc<T, LOG1, LOG2> src{slab, p0};
   ct_fft<T, LOG2, LOGB, false, false, false>(s, f.tw2, src, CtNoDst());
   constexpr int npairs = L1 / 2 + 1;
@@ -58,7 +73,7 @@ __device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *__
     const int k2m = k1 == 0 ? ((L2 - k2) & (L2 - 1)) : (L2 - 1 - k2);
     const C Zk = s[(2 * i + half) * PITCH + cpad16(k2)];
     const C Zm = cconj(s[(2 * i + 1 - half) * PITCH + cpad16(k2m)]);
-    acc_output<T>(e, k, Zk, Zm, Fs);
+    acc_output_tw<T>(e, k, Zk, Zm, Fs, cmul(twr[2 * i + half], twc[k2]));
   }
 }
 
@@ -72,7 +87,7 @@ __global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_rowpass_acc(const ty
 template <typename T, int LOGL> constexpr size_t ct_rowpass_smem() {
   constexpr int LOG2 = LOGL / 2;
   constexpr int B = PassCfg<T>::ELEMS >> LOG2;
-  return sizeof(typename CxOf<T>::type) * (size_t)fft_pitch(1 << LOG2, B) * B;
+  return sizeof(typename CxOf<T>::type) * ((size_t)fft_pitch(1 << LOG2, B) * B + B + (1 << LOG2));
 }
 
 }  // namespace
