@@ -210,13 +210,19 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     }
   }
   const bool seg = nch > 0;
-  // workspace: counts | cursor | offsets | phases or chunk table | records | grid slabs | weights
+  // reserved two-pass binning: CTAs of rspan samples, a table of nrb x ntiles
+  const bool resv = !small && !seg && n > 0 && ntiles <= kScanFuseTiles;
+  const int64_t rspan = resv ? resv_span(n, ntiles) : 0;
+  const int nrb = resv ? (int)((n + rspan - 1) / rspan) : 0;
+  // workspace: counts | cursor | offsets | phases or chunk table | reservations
+  //            | records | grid slabs | weights
   const size_t o_cnt = 0, o_cur = align_up(sizeof(int) * ntiles), o_off = 2 * o_cur;
   const size_t o_phs = o_off + align_up(sizeof(int) * (ntiles + 1));
   const size_t nrec = seg ? 2 * ((size_t)n + CH) : 2 * (size_t)(n > 0 ? n : 1);
-  const size_t o_rec = o_phs + (small ? 0
+  const size_t o_rsv = o_phs + (small ? 0
                                          : (seg ? align_up(sizeof(int) * (size_t)ntiles * nch)
                                                 : align_up(sizeof(uint64_t) * (size_t)(n > 0 ? n : 1))));
+  const size_t o_rec = o_rsv + (resv ? align_up(sizeof(int) * (size_t)nrb * ntiles) : 0);
   const size_t o_grid = o_rec + (small ? 0 : align_up(sizeof(Rec) * nrec));
   const size_t o_wts = o_grid + (small ? 0 : align_up(sizeof(T) * (size_t)p->ng * nslab));
   const size_t bytes = o_wts + (nbs > 0 ? sizeof(T) * (size_t)n * nbs : 0) + 256;
@@ -226,6 +232,7 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   int *counts = (int *)(w + o_cnt), *offsets = (int *)(w + o_off), *cursor = (int *)(w + o_cur);
   uint64_t *phases = (uint64_t *)(w + o_phs);
   int *loc = (int *)(w + o_phs);  // chunk table of the single-pass binning
+  int *rsv = (int *)(w + o_rsv);
   Rec *recs = (Rec *)(w + o_rec);
   T *grid = (T *)(w + o_grid);
   T *wts = multi ? const_cast<T *>(multi) : (nbs > 0 ? (T *)(w + o_wts) : nullptr);
@@ -264,24 +271,21 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   } else {
   // counts and cursor are adjacent: one memset zeroes both
   CUNA_CK(cudaMemsetAsync(counts, 0, o_off, st));
-  if (n > 0 && ntiles <= kScanFuseTiles) {
-    // count (caching each sample's phase), then scan + scatter in one launch
+  if (resv) {
+    // count (caching each sample's phase) and reserve, then scan + scatter
     SampAcc<T> smp{t, y, n, pm, e, phases};
     SampAccS<T> sms{phases, y, n, e};
-    const size_t smc = sizeof(int) * ntiles;
-    const int gcount = (int)std::min<int64_t>((n + 4095) / 4096, 4 * nsm);
-    const int gscat = (int)((n + 512 * kScatterItems - 1) / (512 * kScatterItems));
-    k_bin_count<<<gcount, 512, smc, st>>>(smp, counts, ntiles);
-    CUNA_CK(cudaGetLastError());
-    mark(pr, "bin_count", st);
     static bool attrs = false;
     if (!attrs) {
-      CUNA_CK(cudaFuncSetAttribute(k_bin_scan_scatter<SampAccS<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      CUNA_CK(cudaFuncSetAttribute(k_bin_scatter_resv<SampAccS<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)(sizeof(int) * (3 * kScanFuseTiles + 1))));
       attrs = true;
     }
-    k_bin_scan_scatter<<<gscat, 512, sizeof(int) * (3 * ntiles + 1), st>>>(sms, counts, offsets, cursor, recs,
-                                                                           ntiles);
+    k_bin_count_resv<<<nrb, 512, sizeof(int) * ntiles, st>>>(smp, counts, rsv, ntiles, rspan);
+    CUNA_CK(cudaGetLastError());
+    mark(pr, "bin_count", st);
+    k_bin_scatter_resv<<<nrb, 512, sizeof(int) * (3 * ntiles + 1), st>>>(sms, counts, rsv, offsets, recs, ntiles,
+                                                                         rspan);
     CUNA_CK(cudaGetLastError());
     mark(pr, "bin_scatter", st);
   } else if (n > 0) {

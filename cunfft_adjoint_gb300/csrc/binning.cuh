@@ -12,8 +12,9 @@
 //   k_scan_tiles  exclusive scan counts -> offsets[0..ntiles], cursor = 0
 //   k_bin_scatter per-CTA shared ranks + one global reservation per
 //                 (CTA, tile) -> records in tile order
-//   k_bin_scan_scatter  the last two in one launch (each CTA scans the
-//                 counts itself) for up to kScanFuseTiles tiles
+//   k_bin_count_resv + k_bin_scatter_resv  for up to kScanFuseTiles tiles:
+//                 the count pass also reserves each CTA's range per tile, the
+//                 scatter pass scans the counts itself (see there)
 //   k_bin_local   one pass, records in chunk-local tile order (see there)
 //
 // The tile index of a sample is an exact integer function of its input (the
@@ -27,6 +28,7 @@
 // of all of a thread's samples before computing any of them, so that every
 // warp keeps several global loads in flight.
 #pragma once
+#include <algorithm>
 #include "common.cuh"
 
 namespace cuna {
@@ -200,67 +202,129 @@ __device__ __forceinline__ void cta_exclusive_scan(const int *in, int *out, int 
   __syncthreads();
 }
 
-// k_bin_scan_scatter: k_scan_tiles folded into k_bin_scatter.  Every CTA
-// scans the tile counts itself (ntiles <= kScanFuseTiles ints, from L2) and
-// CTA 0 also publishes offsets[0..ntiles] for the gridding.  cursor[] must be
-// zero on entry.  Launched with 512 threads.
+// Reserved binning for up to kScanFuseTiles tiles, two launches.  Both passes
+// split the samples the same way: CTA b owns [b*span, min((b+1)*span, n)).
+//   k_bin_count_resv    shared histogram of the CTA's tiles; per touched tile
+//                       one returning global atomic on counts[t] reserves the
+//                       CTA's range inside the tile: resv[b*ntiles + t] is its
+//                       start relative to the tile's start.
+//   k_bin_scatter_resv  scans the tile counts itself (CTA 0 publishes
+//                       offsets[0..ntiles]), then ranks each sample with a
+//                       shared atomic and writes its record straight to
+//                       offsets[t] + resv[b*ntiles + t] + rank.
+// The ranks of CTA b in the second pass cover exactly the counts it reserved
+// in the first, so the positions are a permutation of [0, offsets[ntiles]).
+// No global atomic is left in the scatter pass and nothing waits on one.
+// Both are launched with 512 threads; span is a multiple of 512*kCountItems.
 constexpr int kScanFuseTiles = 4096;  // 3 shared arrays of ntiles ints: 48 KB
+constexpr int kResvEntries = 1 << 22; // reservation table limit (ints)
 
 template <class S>
-__global__ void __launch_bounds__(512) k_bin_scan_scatter(S smp, const int *__restrict__ counts,
-                                                          int *__restrict__ offsets, int *__restrict__ cursor,
-                                                          typename S::Rec *__restrict__ recs, int ntiles) {
-  typedef typename S::Rec Rec;
-  extern __shared__ int sh[];
-  int *lc = sh, *lbase = sh + ntiles, *off = sh + 2 * ntiles;  // off: ntiles + 1
-  constexpr int TPT = kScanFuseTiles / 512;  // tiles per thread (blockDim 512)
+__global__ void __launch_bounds__(512) k_bin_count_resv(S smp, int *__restrict__ counts, int *__restrict__ resv,
+                                                        int ntiles, int64_t span) {
+  extern __shared__ int lc[];
+  constexpr int TPT = kScanFuseTiles / 512;
 #pragma unroll
   for (int k = 0; k < TPT; ++k) {
     const int t = threadIdx.x + k * 512;
-    if (t < ntiles) {
-      lc[t] = 0;
-      lbase[t] = counts[t];
+    if (t < ntiles) lc[t] = 0;
+  }
+  __syncthreads();
+  const int64_t beg = (int64_t)blockIdx.x * span, end = min(beg + span, smp.n);
+  for (int64_t c0 = beg; c0 < end; c0 += 512 * kCountItems) {
+    typename S::Raw raw[kCountItems];
+#pragma unroll
+    for (int it = 0; it < kCountItems; ++it) {
+      const int64_t i = c0 + it * 512 + threadIdx.x;
+      if (i < end) raw[it] = smp.load(i, false);
+    }
+#pragma unroll
+    for (int it = 0; it < kCountItems; ++it) {
+      const int64_t i = c0 + it * 512 + threadIdx.x;
+      if (i >= end) continue;
+      Prep<typename S::Rec> p;
+      smp.prep(i, raw[it], p);
+      for (int q = 0; q < p.nt; ++q) atomicAdd(&lc[p.t[q]], 1);
     }
   }
   __syncthreads();
-  cta_exclusive_scan(lbase, off, ntiles);
-  if (blockIdx.x == 0)
-    for (int t = threadIdx.x; t <= ntiles; t += blockDim.x) offsets[t] = off[t];
-  const int64_t chunk0 = (int64_t)blockIdx.x * blockDim.x * kScatterItems;
-  Prep<Rec> p[kScatterItems];
-  int rk[kScatterItems][2];
-  typename S::Raw raw[kScatterItems];
-#pragma unroll
-  for (int it = 0; it < kScatterItems; ++it) {
-    const int64_t i = chunk0 + (int64_t)it * blockDim.x + threadIdx.x;
-    if (i < smp.n) raw[it] = smp.load(i, true);
-  }
-#pragma unroll
-  for (int it = 0; it < kScatterItems; ++it) {
-    const int64_t i = chunk0 + (int64_t)it * blockDim.x + threadIdx.x;
-    p[it].nt = 0;
-    if (i < smp.n) smp.prep(i, raw[it], p[it]);
-    for (int q = 0; q < p[it].nt; ++q) rk[it][q] = atomicAdd(&lc[p[it].t[q]], 1);
-  }
-  __syncthreads();
-  // one reservation per touched tile; all of a thread's reservations are in
-  // flight together before any result is used
   int res[TPT];
 #pragma unroll
   for (int k = 0; k < TPT; ++k) {
     const int t = threadIdx.x + k * 512;
     const int c = t < ntiles ? lc[t] : 0;
-    res[k] = c ? atomicAdd(&cursor[t], c) : 0;
+    res[k] = c ? atomicAdd(&counts[t], c) : 0;
   }
+  int *rv = resv + (int64_t)blockIdx.x * ntiles;
 #pragma unroll
   for (int k = 0; k < TPT; ++k) {
     const int t = threadIdx.x + k * 512;
-    if (t < ntiles && lc[t]) lbase[t] = off[t] + res[k];
+    if (t < ntiles && lc[t]) rv[t] = res[k];
+  }
+}
+
+template <class S>
+__global__ void __launch_bounds__(512) k_bin_scatter_resv(S smp, const int *__restrict__ counts,
+                                                          const int *__restrict__ resv, int *__restrict__ offsets,
+                                                          typename S::Rec *__restrict__ recs, int ntiles,
+                                                          int64_t span) {
+  typedef typename S::Rec Rec;
+  extern __shared__ int sh[];
+  int *lc = sh, *base = sh + ntiles, *off = sh + 2 * ntiles;  // off: ntiles + 1
+  constexpr int TPT = kScanFuseTiles / 512;
+  const int *rv = resv + (int64_t)blockIdx.x * ntiles;
+  int res[TPT];
+#pragma unroll
+  for (int k = 0; k < TPT; ++k) {
+    const int t = threadIdx.x + k * 512;
+    res[k] = 0;
+    if (t < ntiles) {
+      lc[t] = 0;
+      base[t] = counts[t];
+      res[k] = rv[t];  // entries of untouched tiles are stale and never used
+    }
   }
   __syncthreads();
+  cta_exclusive_scan(base, off, ntiles);
+  if (blockIdx.x == 0)
+    for (int t = threadIdx.x; t <= ntiles; t += blockDim.x) offsets[t] = off[t];
 #pragma unroll
-  for (int it = 0; it < kScatterItems; ++it)
-    for (int q = 0; q < p[it].nt; ++q) recs[lbase[p[it].t[q]] + rk[it][q]] = p[it].rec;
+  for (int k = 0; k < TPT; ++k) {
+    const int t = threadIdx.x + k * 512;
+    if (t < ntiles) base[t] = off[t] + res[k];
+  }
+  __syncthreads();
+  const int64_t beg = (int64_t)blockIdx.x * span, end = min(beg + span, smp.n);
+  for (int64_t c0 = beg; c0 < end; c0 += 512 * kCountItems) {
+    typename S::Raw raw[kCountItems];
+#pragma unroll
+    for (int it = 0; it < kCountItems; ++it) {
+      const int64_t i = c0 + it * 512 + threadIdx.x;
+      if (i < end) raw[it] = smp.load(i, true);
+    }
+#pragma unroll
+    for (int it = 0; it < kCountItems; ++it) {
+      const int64_t i = c0 + it * 512 + threadIdx.x;
+      if (i >= end) continue;
+      Prep<Rec> p;
+      smp.prep(i, raw[it], p);
+      for (int q = 0; q < p.nt; ++q) {
+        const int t = p.t[q];
+        recs[base[t] + atomicAdd(&lc[t], 1)] = p.rec;
+      }
+    }
+  }
+}
+
+// Samples per CTA of the reserved binning: at least 512*kCountItems, and
+// enough that the reservation table (CTAs x ntiles ints) stays within
+// kResvEntries.
+inline int64_t resv_span(int64_t n, int ntiles) {
+  const int64_t unit = 512 * kCountItems;
+  const int64_t maxb = std::max<int64_t>(1, kResvEntries / std::max(ntiles, 1));
+  int64_t span = (n + maxb - 1) / maxb;
+  span = std::max(unit, (span + unit - 1) / unit * unit);
+  return span;
 }
 
 // Multi-CTA form of k_scan_tiles for long tile lists: k_scan_blocks scans
