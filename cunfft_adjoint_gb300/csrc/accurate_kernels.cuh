@@ -334,6 +334,31 @@ __device__ __forceinline__ void gauss_cw(T y, T x, T k1, const GaussCW<T, CW> &g
   }
 }
 
+// a[i] += y exp2(-k1 (x + i)^2) for the cells i a record in slot rel = lc - cl0
+// reaches (0 <= rel - i < w2, w2 = 2m), by the centred factorisation of
+// gauss_cw; the mask is applied before the last product so that each tap is
+// one select and one fused multiply-add.
+template <typename T, int CW>
+__device__ __forceinline__ void gauss_acc(T y, T x, T k1, const GaussCW<T, CW> &g, int rel, int w2, T *a) {
+  constexpr int H = CW / 2;
+  const T xc = x + (T)H;
+  const T E = y * exp2_g(-k1 * xc * xc);
+  const T Q = exp2_g((T)(-2) * k1 * xc), Qi = exp2_g((T)2 * k1 * xc);
+  a[H] += (unsigned)(rel - H) < (unsigned)w2 ? E : (T)0;
+  T u = E;
+#pragma unroll
+  for (int j = 1; j < CW - H; ++j) {
+    u *= Q;
+    a[H + j] = fma((unsigned)(rel - H - j) < (unsigned)w2 ? u : (T)0, g.c[j], a[H + j]);
+  }
+  u = E;
+#pragma unroll
+  for (int j = 1; j <= H; ++j) {
+    u *= Qi;
+    a[H - j] = fma((unsigned)(rel - H + j) < (unsigned)w2 ? u : (T)0, g.c[j], a[H - j]);
+  }
+}
+
 __device__ __forceinline__ void store4(float *p, float a, float b, float c, float d) {
   *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
 }
@@ -504,25 +529,23 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
         T a[1][CW];
 #pragma unroll
         for (int i = 0; i < CW; ++i) a[0][i] = (T)0;
-        const int ctr = cl0 + m;
-        const unsigned w2 = (unsigned)(2 * m);
+        const int ctr = cl0 + m, w2 = 2 * m;
         for (int r = rb; r < re; ++r) {
           const SRec<T> rr = srec[r];
           const int rel = rr.lc - cl0;            // lc - c for c = cl0
           const T dd0 = (T)(ctr - rr.lc) - rr.f;  // d - f for c = cl0
-          T w[CW];
-          gauss_cw<T, CW>(SG > 1 ? (T)1 : rr.y, dd0, e.k1, gw, w);
-#pragma unroll
-          for (int i = 0; i < CW; ++i) w[i] = (unsigned)(rel - i) < w2 ? w[i] : (T)0;
           if constexpr (SG == 1) {
-#pragma unroll
-            for (int i = 0; i < CW; ++i) a[0][i] += w[i];
+            gauss_acc<T, CW>(rr.y, dd0, e.k1, gw, rel, w2, a[0]);
           } else {
+            T w[CW];
+            gauss_cw<T, CW>((T)1, dd0, e.k1, gw, w);
+#pragma unroll
+            for (int i = 0; i < CW; ++i) w[i] = (unsigned)(rel - i) < (unsigned)w2 ? w[i] : (T)0;
 #pragma unroll
             for (int g = 0; g < SG; ++g) {
               const T yg = yv[g * CAP + r];
 #pragma unroll
-              for (int i = 0; i < CW; ++i) acc[g][i] += yg * w[i];
+              for (int i = 0; i < CW; ++i) acc[g][i] = fma(yg, w[i], acc[g][i]);
             }
           }
         }
