@@ -273,6 +273,31 @@ def test_host_async_two_streams(nfft):
         assert rel_l2(Fh[s].numpy(), ref.cpu().numpy()) < 1e-6
 
 
+def test_reserved_binning_many_blocks(nfft, oracle_lib):
+    """10,000,001 unsorted samples on 2048 tiles: the two-launch reserved
+    binning runs each block over two sub-chunks of 4096 samples (its
+    reservation table holds 2^22 entries) with a ragged last block; the
+    spectrum equals the one binned by the three-launch form (8192 tiles,
+    more than the fused scan takes) and the NDFT."""
+    from cunfft_adjoint_gb300 import _lib
+    rng = np.random.default_rng(77)
+    n, nf, T = 10_000_001, 1 << 20, 1000.0
+    t = rng.uniform(0, T, n)
+    y = rng.normal(0, 1, n).astype(np.float32)
+    td = torch.as_tensor(t, device="cuda")
+    yd = torch.as_tensor(y, device="cuda")
+    plan = nfft.AdjointNFFT(nf, 4, 12, torch.float32)
+    plan.binning = _lib.BIN_GLOBAL
+    plan.set_schedule(11, _lib.GRID_GATHER)
+    F1 = plan(td, yd, 0.0, T).cpu().numpy().astype(np.complex128)
+    plan.set_schedule(9, _lib.GRID_GATHER)
+    F2 = plan(td, yd, 0.0, T).cpu().numpy().astype(np.complex128)
+    assert rel_l2(F1, F2) < 2e-6
+    k = np.sort(rng.choice(np.arange(-nf // 2, nf // 2), 32, replace=False))
+    D = oracle_lib.ndft(t, y.astype(np.float64), 0.0, T, k)
+    assert rel_l2(F1[k + nf // 2], D) < 1e-5
+
+
 @pytest.mark.parametrize("dtype,nf,R,tol", [(torch.float32, 1 << 24, 4, 1e-5), (torch.float64, 1 << 22, 4, 1e-9)])
 def test_largest_plans(nfft, oracle_lib, dtype, nf, R, tol):
     """The largest grids a plan accepts (2^25 packed points float, 2^23
