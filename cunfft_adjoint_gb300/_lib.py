@@ -48,6 +48,7 @@ CORE_SIGNATURES = {
     "cuna2_last_error": (ctypes.c_char_p, []),
     "cuna2_status_string": (ctypes.c_char_p, [_I]),
     "cuna2_version": (ctypes.c_char_p, []),
+    "cuna2_wait_timeouts": (ctypes.c_longlong, []),
     "cuna2_compat_filter_radius": (_I, [_I]),
     "cuna2_compat_filter_f32": (_I, [_P, _I, _I, _P, _P, _P]),
     "cuna2_compat_filter_f64": (_I, [_P, _I, _I, _P, _P, _P]),

@@ -133,8 +133,7 @@ template <typename T, int LOGL>
 int ct_passes_at(typename CxOf<T>::type *z, const FftDev<T> &f, const AccParams<T> &e, typename CxOf<T>::type *F,
                  int nslab, cudaStream_t st, Prof *pr) {
   constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
-  constexpr int BA = PassCfg<T>::ELEMS >> LOG1, BB = PassCfg<T>::ELEMS >> LOG2, PB = BB / 2;
-  constexpr int npairs = (1 << LOG1) / 2 + 1;
+  constexpr int BA = PassCfg<T>::ELEMS >> LOG1;
   constexpr size_t smA = ct_colpass_smem<T, LOGL>(), smB = ct_rowpass_smem<T, LOGL>();
   static bool attr = false;
   if (!attr) {
@@ -143,10 +142,29 @@ int ct_passes_at(typename CxOf<T>::type *z, const FftDev<T> &f, const AccParams<
       return -1;
     attr = true;
   }
-  k_ct_colpass<T, LOGL><<<dim3((1 << LOG2) / BA, nslab), PassCfg<T>::THREADS, smA, st>>>(z, f, (int64_t)1 << LOGL);
+  bool tma = false;
+  if constexpr (sizeof(T) == 4 && TmaCol<LOGL>::ok) {
+    // column pass through TMA boxes when the driver encodes the tensor map
+    int *tmo = tma_enabled() ? wait_timeout_counter() : nullptr;
+    alignas(64) CUtensorMap map;
+    if (tmo && ct_colpass_tma_map<LOGL>(&map, z, nslab)) {
+      static bool attr_tma = false;
+      if (!attr_tma) {
+        if (cudaFuncSetAttribute(k_ct_colpass_tma<LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)ct_colpass_tma_smem<LOGL>()))
+          return -1;
+        attr_tma = true;
+      }
+      k_ct_colpass_tma<LOGL><<<dim3((1 << LOG2) / BA, nslab), PassCfg<T>::THREADS, ct_colpass_tma_smem<LOGL>(), st>>>(
+          map, f, tmo);
+      tma = true;
+    }
+  }
+  if (!tma)
+    k_ct_colpass<T, LOGL><<<dim3((1 << LOG2) / BA, nslab), PassCfg<T>::THREADS, smA, st>>>(z, f, (int64_t)1 << LOGL);
   if (cudaPeekAtLastError() != cudaSuccess) return -1;
   mark(pr, "fft_colpass", st);
-  k_ct_rowpass_acc<T, LOGL><<<dim3((npairs + PB - 1) / PB, nslab), PassCfg<T>::THREADS, smB, st>>>(z, f, e, F);
+  k_ct_rowpass_acc<T, LOGL><<<dim3(ct_rowpass_ctas<T, LOGL>(), nslab), PassCfg<T>::THREADS, smB, st>>>(z, f, e, F);
   if (cudaPeekAtLastError() != cudaSuccess) return -1;
   mark(pr, "fft_rowpass", st);
   return 1;

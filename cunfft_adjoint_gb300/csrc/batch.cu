@@ -165,8 +165,7 @@ __global__ void __launch_bounds__(PassCfg<T>::THREADS) k_bct_rowpass(const T *gr
 template <typename T, int LOGL>
 int bct_at(T *grid, const BDesc<T> *D, const int *list, int cnt, typename CxOf<T>::type *F, cudaStream_t st) {
   constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
-  constexpr int BA = PassCfg<T>::ELEMS >> LOG1, BB = PassCfg<T>::ELEMS >> LOG2, PB = BB / 2;
-  constexpr int npairs = (1 << LOG1) / 2 + 1;
+  constexpr int BA = PassCfg<T>::ELEMS >> LOG1;
   constexpr size_t smA = ct_colpass_smem<T, LOGL>(), smB = ct_rowpass_smem<T, LOGL>();
   static bool attr = false;
   if (!attr) {
@@ -177,7 +176,7 @@ int bct_at(T *grid, const BDesc<T> *D, const int *list, int cnt, typename CxOf<T
   }
   k_bct_colpass<T, LOGL><<<dim3((1 << LOG2) / BA, cnt), PassCfg<T>::THREADS, smA, st>>>(grid, D, list);
   if (cudaPeekAtLastError() != cudaSuccess) return -1;
-  k_bct_rowpass<T, LOGL><<<dim3((npairs + PB - 1) / PB, cnt), PassCfg<T>::THREADS, smB, st>>>(grid, D, list, F);
+  k_bct_rowpass<T, LOGL><<<dim3(ct_rowpass_ctas<T, LOGL>(), cnt), PassCfg<T>::THREADS, smB, st>>>(grid, D, list, F);
   if (cudaPeekAtLastError() != cudaSuccess) return -1;
   return 1;
 }

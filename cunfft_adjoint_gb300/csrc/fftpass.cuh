@@ -9,18 +9,22 @@ namespace cuna {
 namespace {
 
 // ---------------------------------------------------------------------------
-// row pass with the accurate epilogue: a CTA owns row pairs (p, L1 - p),
-// p in [p0, p0 + B/2), transforms them (length L2) into shared memory, then
-// unpacks, deconvolves and centres every output k = k1 + L1 k2 <= K.
+// row pass with the accurate epilogue: a CTA owns the row-pair slots
+// p in [p0, p0 + B/2), transforms their rows (length L2) into shared memory,
+// then unpacks, deconvolves and centres every output k = k1 + L1 k2 <= K.
+// Slot p >= 1 holds rows (p, L1 - p), whose outputs need each other's
+// values; rows 0 and L1/2 each pair with themselves and share slot 0, so
+// there are exactly L1/2 slots and every CTA's slots are all used.
 // ---------------------------------------------------------------------------
+template <int LOG1> __host__ __device__ constexpr int ct_pair_row(int p, int half) {
+  return half ? (p == 0 ? (1 << LOG1) / 2 : (1 << LOG1) - p) : p;
+}
+
 template <typename T, int LOG1, int LOG2> struct CtPairSrc {
   const typename CxOf<T>::type *p;  // slab
   int p0;
   __device__ __forceinline__ typename CxOf<T>::type load(int seq, int j, int dr) const {
-    constexpr int L1 = 1 << LOG1;
-    const int pp = p0 + (seq >> 1);
-    const int row = (seq & 1) ? ((L1 - pp) & (L1 - 1)) : pp;
-    return pp <= L1 / 2 ? p[(row << LOG2) + j + dr] : cmk((T)0, (T)0);
+    return p[(ct_pair_row<LOG1>(p0 + (seq >> 1), seq & 1) << LOG2) + j + dr];
   }
 };
 
@@ -34,7 +38,7 @@ __device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *__
                                                 const AccParams<T> &e, typename CxOf<T>::type *Fs, int pblock) {
   typedef typename CxOf<T>::type C;
   constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
-  constexpr int L1 = 1 << LOG1, L2 = 1 << LOG2;
+  constexpr int L2 = 1 << LOG2;
   constexpr int LOGB = ilog2c(PassCfg<T>::ELEMS) - LOG2;
   constexpr int B = 1 << LOGB, LOGP = LOGB - 1, P = B >> 1;
   constexpr int PITCH = fft_pitch(L2, B);
@@ -46,33 +50,26 @@ __device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *__
   C *twr = s + PITCH * B, *twc = twr + B;
   const int p0 = pblock * P;
   for (int u = threadIdx.x; u < B + L2; u += THREADS) {
-    int q;
-    if (u < B) {
-      const int pp = p0 + (u >> 1);
-      q = (u & 1) ? ((L1 - pp) & (L1 - 1)) : pp;
-    } else {
-      q = (u - B) << LOG1;
-    }
+    const int q = u < B ? ct_pair_row<LOG1>(p0 + (u >> 1), u & 1) : (u - B) << LOG1;
     T sn, cs;
     sincospi_t((T)q * e.twk, &sn, &cs);
     twr[u] = cmk(cs, sn);  // twr[B + k2] is twc[k2]
   }
   CtPairSrc<T, LOG1, LOG2> src{slab, p0};
   ct_fft<T, LOG2, LOGB, false, false, false>(s, f.tw2, src, CtNoDst());
-  constexpr int npairs = L1 / 2 + 1;
 #pragma unroll 4
   for (int idx = threadIdx.x; idx < (B << LOG2); idx += THREADS) {
     const int i = idx & (P - 1), half = (idx >> LOGP) & 1, k2 = idx >> (LOGP + 1);
     const int p = p0 + i;
-    if (p >= npairs) continue;
-    const int rowA = p, rowB = (L1 - p) & (L1 - 1);
-    if (half && rowA == rowB) continue;
-    const int k1 = half ? rowB : rowA;
+    const int k1 = ct_pair_row<LOG1>(p, half);
     const int64_t k = (int64_t)k1 + ((int64_t)k2 << LOG1);
     if (k > e.K) continue;
+    // Z[L - k] is in row (L1 - k1) mod L1: the slot's other row, or the
+    // same row for the self-paired rows 0 and L1/2 of slot 0
     const int k2m = k1 == 0 ? ((L2 - k2) & (L2 - 1)) : (L2 - 1 - k2);
+    const int seqm = p == 0 ? 2 * i + half : 2 * i + 1 - half;
     const C Zk = s[(2 * i + half) * PITCH + cpad16(k2)];
-    const C Zm = cconj(s[(2 * i + 1 - half) * PITCH + cpad16(k2m)]);
+    const C Zm = cconj(s[seqm * PITCH + cpad16(k2m)]);
     acc_output_tw<T>(e, k, Zk, Zm, Fs, cmul(twr[2 * i + half], twc[k2]));
   }
 }
@@ -82,6 +79,11 @@ __global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_rowpass_acc(const ty
                                                                         FftDev<T> f, AccParams<T> e,
                                                                         typename CxOf<T>::type *F) {
   ct_rowpass_body<T, LOGL>(grid + ((int64_t)blockIdx.y << LOGL), f, e, F + (int64_t)blockIdx.y * e.nf, blockIdx.x);
+}
+
+// CTAs per packed grid of the row pass: L1/2 slots, B/2 per CTA
+template <typename T, int LOGL> constexpr int ct_rowpass_ctas() {
+  return ((1 << ((LOGL + 1) / 2)) / 2) / ((PassCfg<T>::ELEMS >> (LOGL / 2)) / 2);
 }
 
 template <typename T, int LOGL> constexpr size_t ct_rowpass_smem() {

@@ -13,8 +13,10 @@
 // its W_L^{c k} twiddles as (per-butterfly base) x (per-CTA table of 16 x B
 // steps in shared memory) instead of two global table reads per value.
 #pragma once
+#include <type_traits>
 #include "fft.cuh"
 #include "runtime.h"
+#include "tma.cuh"
 
 namespace cuna {
 namespace {
@@ -26,6 +28,11 @@ template <int R> struct RLog {
 };
 
 __host__ __device__ constexpr int cpad16(int i) { return i + (i >> 4); }
+
+// Sources and destinations that live in the stage's own shared buffer
+// (kShared = true) need a barrier between the stage's reads and its writes.
+template <class X, class = void> struct in_smem : std::false_type {};
+template <class X> struct in_smem<X, std::void_t<decltype(X::kShared)>> : std::bool_constant<X::kShared> {};
 
 template <typename T> struct PassCfg {
   static constexpr int ELEMS = sizeof(T) == 4 ? kPassElemsF32 : kPassElemsF64;
@@ -91,7 +98,7 @@ __device__ __forceinline__ void ct_stage(typename CxOf<T>::type *s, const typena
     }
     dftR<R>(v[u]);
   }
-  if (!IN_G && !OUT_G) __syncthreads();
+  if ((!IN_G || in_smem<Src>::value) && (!OUT_G || in_smem<Dst>::value)) __syncthreads();
 #pragma unroll
   for (int u = 0; u < NB; ++u) {
     const int g = threadIdx.x + u * THREADS;
@@ -207,6 +214,106 @@ template <typename T, int LOGL> constexpr size_t ct_colpass_smem() {
   constexpr int LOG1 = (LOGL + 1) / 2;
   constexpr int B = PassCfg<T>::ELEMS >> LOG1;
   return sizeof(typename CxOf<T>::type) * ((size_t)fft_pitch(1 << LOG1, B) * B + 17 * B);
+}
+
+// ---------------------------------------------------------------------------
+// column pass with TMA (float, B >= 2 columns per CTA): the CTA's B columns
+// (L1 rows x 8B bytes, one row every L2 complex) come in as L1/256 boxes of a
+// 3D tensor map {2 L2 floats, L1 rows, slabs} into shared memory, row-major
+// [row][column] ("dense"); the first stage reads them from there, the last
+// stage writes the twiddled result back in the same dense order and the
+// boxes go out with TMA stores.  No strided global access is left to the
+// load/store units.  A copy that does not complete within the bounded wait
+// is counted in `timeouts` and the CTA leaves its columns unwritten.
+// ---------------------------------------------------------------------------
+template <typename T, int LOGB> struct CtDenseSrc {
+  static constexpr bool kShared = true;
+  const typename CxOf<T>::type *s;
+  __device__ __forceinline__ typename CxOf<T>::type load(int seq, int j, int dr) const {
+    return s[((j + dr) << LOGB) + seq];
+  }
+};
+
+template <typename T, int LOGB> struct CtDenseDst {
+  static constexpr bool kShared = true;
+  typename CxOf<T>::type *s;
+  const typename CxOf<T>::type *steps;  // shared: steps[seq * 17 + r] = W_L^{c (r << LOGNS_last)}
+  FftDev<T> f;
+  int c0;
+  template <int R, int LOGNS>
+  __device__ __forceinline__ void store(int seq, int idxD, typename CxOf<T>::type *v) const {
+    typedef typename CxOf<T>::type C;
+    static_assert(R == 16 || LOGNS == 0, "the storing stage is radix 16 or the only stage");
+    const C w0 = twiddle_L(f, (c0 + seq) * idxD);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const C w = r == 0 ? w0 : cmul(w0, steps[seq * 17 + r]);
+      s[((idxD + (r << LOGNS)) << LOGB) + seq] = cmul(v[r], w);
+    }
+  }
+};
+
+template <int LOGL> struct TmaCol {
+  static constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
+  static constexpr int LOGB = ilog2c(PassCfg<float>::ELEMS) - LOG1;
+  static constexpr int B = 1 << LOGB;
+  static constexpr int ROWS = (1 << LOG1) < 256 ? (1 << LOG1) : 256;  // rows per box
+  static constexpr int NBOX = (1 << LOG1) / ROWS;
+  static constexpr bool ok = B >= 2;  // box rows of >= 16 bytes
+};
+
+template <int LOGL>
+__global__ void __launch_bounds__(PassCfg<float>::THREADS) k_ct_colpass_tma(const __grid_constant__ CUtensorMap map,
+                                                                           FftDev<float> f, int *timeouts) {
+  typedef TmaCol<LOGL> G;
+  typedef typename CxOf<float>::type C;
+  constexpr int LOG1 = G::LOG1, LOGB = G::LOGB, B = G::B;
+  constexpr int PITCH = fft_pitch(1 << LOG1, B);
+  constexpr int LNS = last_logns<LOG1>();
+  static_assert(G::ok, "TMA column pass needs two columns per CTA");
+  extern __shared__ __align__(128) unsigned char smem_tma[];
+  C *s = reinterpret_cast<C *>(smem_tma);
+  C *steps = s + PITCH * B;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(steps + 17 * B);
+  const int c0 = blockIdx.x * B, slab = blockIdx.y;
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(bar, (uint32_t)(sizeof(C) << (LOG1 + LOGB)));
+#pragma unroll 1
+    for (int b = 0; b < G::NBOX; ++b) tma_load_3d(s + b * G::ROWS * B, &map, 2 * c0, b * G::ROWS, slab, bar);
+  }
+  for (int i = threadIdx.x; i < 16 * B; i += PassCfg<float>::THREADS)
+    steps[(i >> 4) * 17 + (i & 15)] = twiddle_L(f, (c0 + (i >> 4)) * ((i & 15) << LNS));
+  if (!__syncthreads_and(mbar_wait(bar, 0))) {
+    if (threadIdx.x == 0) atomicAdd(timeouts, 1);
+    return;
+  }
+  CtDenseSrc<float, LOGB> src{s};
+  CtDenseDst<float, LOGB> dst{s, steps, f, c0};
+  ct_fft<float, LOG1, LOGB, true, true, true>(s, f.tw1, src, dst);
+  fence_proxy_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll 1
+    for (int b = 0; b < G::NBOX; ++b) tma_store_3d(&map, 2 * c0, b * G::ROWS, slab, s + b * G::ROWS * B);
+    bulk_commit();
+    bulk_wait_all();
+  }
+}
+
+template <int LOGL> constexpr size_t ct_colpass_tma_smem() { return ct_colpass_smem<float, LOGL>() + 16; }
+
+// The tensor map of k_ct_colpass_tma for `nslab` packed grids of L = 2^LOGL
+// complex at `z` (slab stride L).
+template <int LOGL> bool ct_colpass_tma_map(void *map, const void *z, int nslab) {
+  typedef TmaCol<LOGL> G;
+  const uint64_t L2 = 1ull << G::LOG2, L1 = 1ull << G::LOG1;
+  return encode_tmap_f32_3d(map, z, 2 * L2, L1, (uint64_t)nslab, 2 * L2 * sizeof(float),
+                            (L1 * L2) * 2 * sizeof(float), 2 * G::B, G::ROWS);
 }
 
 }  // namespace

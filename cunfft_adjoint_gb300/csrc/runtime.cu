@@ -7,6 +7,9 @@
 #include <string>
 #include <tuple>
 #include <vector>
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <stdlib.h>
 #include "runtime.h"
 
 namespace cuna {
@@ -173,3 +176,67 @@ extern "C" const char *cuna2_status_string(int s) {
 }
 
 extern "C" const char *cuna2_version(void) { return "cuna-gb300 1.0 (sm_103a)"; }
+
+namespace cuna {
+namespace {
+int *g_timeouts_host = nullptr;
+int *g_timeouts_dev = nullptr;
+std::once_flag g_timeouts_once;
+}  // namespace
+
+int *wait_timeout_counter() {
+  std::call_once(g_timeouts_once, [] {
+    int *h = nullptr, *d = nullptr;
+    if (cudaHostAlloc((void **)&h, sizeof(int), cudaHostAllocMapped) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    *h = 0;
+    if (cudaHostGetDevicePointer((void **)&d, h, 0) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFreeHost(h);
+      return;
+    }
+    g_timeouts_host = h;
+    g_timeouts_dev = d;
+  });
+  return g_timeouts_dev;
+}
+
+bool tma_enabled() {
+  static const bool on = [] {
+    const char *v = getenv("CUNA2_TMA");
+    return v && v[0] == '1';
+  }();
+  return on;
+}
+
+bool encode_tmap_f32_3d(void *map, const void *base, uint64_t d0, uint64_t d1, uint64_t d2, uint64_t s1,
+                        uint64_t s2, uint32_t b0, uint32_t b1) {
+  static PFN_cuTensorMapEncodeTiled_v12000 enc = [] {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    }
+    return (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {d0, d1, d2};
+  const cuuint64_t strides[2] = {s1, s2};
+  const cuuint32_t box[3] = {b0, b1, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(reinterpret_cast<CUtensorMap *>(map), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(base),
+             dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace cuna
+
+extern "C" long long cuna2_wait_timeouts(void) {
+  cuna::wait_timeout_counter();
+  return cuna::g_timeouts_host ? (long long)*(volatile int *)cuna::g_timeouts_host : 0;
+}

@@ -58,4 +58,21 @@ constexpr int kMaxLogL = 26;
 // hold the whole transform (multi-CTA passes for a single small transform)
 int fft_geometry(bool is_double, int logL, FftGeom *g, bool split = false);
 
+// Device pointer (host-mapped) of the counter of bounded waits that ran out;
+// nullptr when mapped host memory is unavailable (TMA kernels are then not
+// used).
+int *wait_timeout_counter();
+// The TMA column pass is used when the environment sets CUNA2_TMA=1.  It
+// gives bit-identical spectra; measured on GB300 it ties the load/store
+// column pass where the grid is L2-resident and is slower (101 against 88 us
+// for 1024 grids of 2^15 points) where the pass streams from HBM, because a
+// CTA can start its transform only once all its boxes have landed.
+bool tma_enabled();
+// Tiled 3D tensor map (CUtensorMap, 128 bytes at `map`) over float32 data at
+// `base`: dims {d0, d1, d2} (d0 innermost), byte strides {s1, s2} of
+// dimensions 1 and 2, box {b0, b1, 1}.  Returns false when the driver entry
+// point is missing or the encoding is rejected.
+bool encode_tmap_f32_3d(void *map, const void *base, uint64_t d0, uint64_t d1, uint64_t d2, uint64_t s1,
+                        uint64_t s2, uint32_t b0, uint32_t b1);
+
 }  // namespace cuna

@@ -46,6 +46,10 @@ const char *cuna2_last_error(void);
 const char *cuna2_status_string(int status);
 /* Library version string. */
 const char *cuna2_version(void);
+/* Number of bounded device waits (TMA copy completions) that ran out since
+   the process started; 0 in normal operation.  A kernel whose wait runs out
+   counts it here and leaves its output unwritten instead of waiting on. */
+long long cuna2_wait_timeouts(void);
 
 /* ---------------------------------------------------------------------- */
 /* compat mode: the reference library's arithmetic                         */
