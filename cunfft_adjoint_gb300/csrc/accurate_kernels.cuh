@@ -692,22 +692,6 @@ __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 3) k_grid_s
 // 2^62 (double, int64 cells) units, the quantum is 2^-30 (2^-62) of the
 // bound.  Integer sums do not depend on the order of the atomics, so the grid
 // is bit-reproducible run to run.  A non-finite value makes its tiles NaN.
-template <typename T> struct FixAcc;
-template <> struct FixAcc<float> {
-  typedef int type;
-  static constexpr float range = 1073741824.0f;  // 2^30
-  __device__ static int to_fix(float w) { return __float2int_rn(w); }
-  __device__ static void add(int *a, int v) { atomicAdd(a, v); }
-};
-template <> struct FixAcc<double> {
-  typedef long long type;
-  static constexpr double range = 4611686018427387904.0;  // 2^62
-  __device__ static long long to_fix(double w) { return __double2ll_rn(w); }
-  __device__ static void add(long long *a, long long v) {
-    atomicAdd(reinterpret_cast<unsigned long long *>(a), (unsigned long long)v);
-  }
-};
-
 // records [c0, c0 + cnt) -> srec (values from ws when given); returns the
 // thread's max |value| (NaN once one is not finite)
 template <typename T, class Src>

@@ -56,4 +56,24 @@ __host__ __device__ __forceinline__ int ilog2i(int64_t v) {
   return r;
 }
 
+// Fixed-point accumulation in shared memory: a value w (already scaled so
+// that every cell's sum stays within `range`) is rounded to an integer and
+// added with a native shared-memory integer atomic; integer sums do not
+// depend on the order of the atomics.
+template <typename T> struct FixAcc;
+template <> struct FixAcc<float> {
+  typedef int type;
+  static constexpr float range = 1073741824.0f;  // 2^30
+  __device__ static int to_fix(float w) { return __float2int_rn(w); }
+  __device__ static void add(int *a, int v) { atomicAdd(a, v); }
+};
+template <> struct FixAcc<double> {
+  typedef long long type;
+  static constexpr double range = 4611686018427387904.0;  // 2^62
+  __device__ static long long to_fix(double w) { return __double2ll_rn(w); }
+  __device__ static void add(long long *a, long long v) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(a), (unsigned long long)v);
+  }
+};
+
 }  // namespace cuna

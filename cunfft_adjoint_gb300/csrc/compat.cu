@@ -8,7 +8,7 @@
 // Pipeline per call (all on the caller's stream, no host synchronisation):
 //   k_bin_count / k_scan_tiles / k_bin_scatter  samples -> tile-sorted records
 //   k_grid_compat     one CTA per (tile, resample): taps accumulated in shared
-//                     memory, flushed once with f_hat[c].x += acc[c]
+//                     memory in fixed point, flushed once with f_hat[c].x += acc[c]
 //   FFT               in-place inverse FFT of ng points with the reference's
 //                     deconvolution fused into the last pass
 //                     (single CTA for ng <= 2^14 (f32) / 2^13 (f64), four-step
@@ -155,64 +155,145 @@ __device__ __forceinline__ double rec_val(const RecD &r) { return r.v; }
 
 // ---------------------------------------------------------------------------
 // tiled gridding: fast_gridding / fast_gridding_bootstrap,
-// src/gridding.cu:36-65,86-117
+// src/gridding.cu:36-65,86-117.  Every tap weight is the reference's own
+// expression val * (E1 * pow(E2, m) * E3[|m|]) (filter(),
+// src/gaussian_filter.cu:264-273); only the summation differs: instead of
+// float atomics into f_hat (order-dependent) each CTA sums its tile in
+// fixed point with native shared integer atomics and adds the tile to f_hat
+// once.  The tile's scale comes from a bound on every cell's sum: |val| <=
+// Ymax over the tile's records, a weight is at most 1 / sqrt(pi b), and at
+// most 2 hmax records reach one cell (hmax: the most records in a bucket of
+// >= 2 rf cells).  The quantum is 2^-30 (float) / 2^-62 (double) of that
+// bound, and the sums no longer depend on the order of the atomics.
 // ---------------------------------------------------------------------------
 template <typename T, bool BOOT>
-__global__ void __launch_bounds__(256) k_grid_compat(const typename RecOf<T>::type *__restrict__ recs,
-                                                     const int *__restrict__ off,
-                                                     typename CxOf<T>::type *f_hat, int ng,
-                                                     const typename FpOf<T>::type *fp,
-                                                     const T *__restrict__ y, int n, unsigned seed) {
+__device__ __forceinline__ void compat_coefs(const typename RecOf<T>::type &rc, const T *E1g, const T *E2g,
+                                             const T *y, int n, unsigned seed, int slab, T &E1, T &E2, T &val) {
+  if (BOOT) {
+    const int i = slab * n + rc.p;
+    int d = rc.p;
+    val = (T)1.0;
+    if (y) {
+      d = xorshift32(wang_hash(seed + i)) % n;
+      val = y[d];
+    }
+    E1 = E1g[d];
+    E2 = E2g[d];
+  } else {
+    E1 = rc.a;
+    E2 = rc.b;
+    val = rec_val(rc);
+  }
+}
+
+constexpr int kCompatThreads = 256;
+
+template <typename T, bool BOOT>
+__global__ void __launch_bounds__(kCompatThreads) k_grid_compat(const typename RecOf<T>::type *__restrict__ recs,
+                                                                const int *__restrict__ off,
+                                                                typename CxOf<T>::type *f_hat, int ng,
+                                                                const typename FpOf<T>::type *fp,
+                                                                const T *__restrict__ y, int n, unsigned seed) {
   typedef typename RecOf<T>::type Rec;
+  typedef FixAcc<T> FA;
+  typedef typename FA::type A;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *acc = reinterpret_cast<T *>(smem_raw);
-  T *e3 = acc + (1 << kCompatLogTL);
+  A *acc = reinterpret_cast<A *>(smem_raw);
+  T *e3 = reinterpret_cast<T *>(acc + (1 << kCompatLogTL));
+  int *hist = reinterpret_cast<int *>(e3 + kCompatMaxRf);
+  __shared__ float red[kCompatThreads / 32];
+  __shared__ int redi[kCompatThreads / 32];
+  __shared__ T scale_s;
   const int tile = blockIdx.x, slab = blockIdx.y;
   const int base = tile << kCompatLogTL;
   const int tl = min(1 << kCompatLogTL, ng - base);
   const int rf = fp->filter_radius;
-  const T *E3g = fp->E3;
-  for (int c = threadIdx.x; c < tl; c += blockDim.x) acc[c] = (T)0;
-  for (int m = threadIdx.x; m < rf && m < kCompatMaxRf; m += blockDim.x) e3[m] = E3g[m];
+  const T *E3g = fp->E3, *E1g = fp->E1, *E2g = fp->E2;
+  // buckets of >= 2 rf cells: the records reaching one cell lie in two buckets
+  int logBS = 4;
+  while ((1 << logBS) < 2 * rf) ++logBS;
+  const int NB = ((tl + 2 * rf) >> logBS) + 1;
+  for (int c = threadIdx.x; c < tl; c += kCompatThreads) acc[c] = 0;
+  for (int m = threadIdx.x; m < rf && m < kCompatMaxRf; m += kCompatThreads) e3[m] = E3g[m];
+  for (int q = threadIdx.x; q < NB; q += kCompatThreads) hist[q] = 0;
   __syncthreads();
-  const T *E1g = fp->E1, *E2g = fp->E2;
-  const int r1 = off[tile + 1];
-  for (int r = off[tile] + threadIdx.x; r < r1; r += blockDim.x) {
+  const int r0 = off[tile], r1 = off[tile + 1];
+  // bound pass: records per bucket and the largest |value| (NaN if any is not finite)
+  float ym = 0.f;
+  for (int r = r0 + threadIdx.x; r < r1; r += kCompatThreads) {
     const Rec rc = recs[r];
-    const int j = rc.cell;
-    int ms = -rf + 1, me = rf;
-    if (j + ms < 0) ms = -j;
-    if (j + me > ng) me = ng - j;
+    atomicAdd(&hist[(rc.cell - base + rf) >> logBS], 1);
     T E1, E2, val;
-    if (BOOT) {
-      const int i = slab * n + rc.p;
-      int d = rc.p;
-      val = (T)1.0;
-      if (y) {
-        d = xorshift32(wang_hash(seed + i)) % n;
-        val = y[d];
-      }
-      E1 = E1g[d];
-      E2 = E2g[d];
-    } else {
-      E1 = rc.a;
-      E2 = rc.b;
-      val = rec_val(rc);
+    compat_coefs<T, BOOT>(rc, E1g, E2g, y, n, seed, slab, E1, E2, val);
+    ym = isfinite(val) && !isnan(ym) ? fmaxf(ym, (float)fabs(val)) : __int_as_float(0x7fffffff);
+  }
+  __syncthreads();
+  int hmax = 0;
+  for (int q = threadIdx.x; q < NB; q += kCompatThreads) hmax = max(hmax, hist[q]);
+  for (int o = 16; o > 0; o >>= 1) {
+    hmax = max(hmax, __shfl_xor_sync(0xffffffffu, hmax, o));
+    const float u = __shfl_xor_sync(0xffffffffu, ym, o);
+    ym = (isnan(u) || isnan(ym)) ? __int_as_float(0x7fffffff) : fmaxf(ym, u);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    redi[threadIdx.x >> 5] = hmax;
+    red[threadIdx.x >> 5] = ym;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int h = 0;
+    float v = 0.f;
+    bool bad = false;
+    for (int w = 0; w < kCompatThreads / 32; ++w) {
+      h = max(h, redi[w]);
+      bad |= isnan(red[w]);
+      v = fmaxf(v, red[w]);
     }
-    const int lo = max(ms, base - j), hi = min(me, base + tl - j);
-    for (int m = lo; m < hi; ++m) {
-      const int mp = m < 0 ? -m : m;
-      const T e3m = mp < kCompatMaxRf ? e3[mp] : E3g[mp];
-      const T w = val * (E1 * cpow(E2, m) * e3m);
-      atomicAdd(&acc[j + m - base], w);
+    // a tap weight E1 E2^m E3[|m|] = exp(-(eps - m)^2 / b) / sqrt(pi b) is at
+    // most 1 / sqrt(pi b); 1% margin for the approximate exp and pow
+    const T wmax = (T)1.01 / sqrt((T)CUNA_PI * fp->b);
+    const T B = (T)v * wmax * (T)(2 * h);
+    T sc = B > (T)0 ? FA::range / B : (T)0;
+    if (isinf(sc)) sc = (T)0;
+    scale_s = bad ? (T)NAN : sc;
+  }
+  __syncthreads();
+  const T sc = scale_s;
+  if (sc > (T)0) {
+    for (int r = r0 + threadIdx.x; r < r1; r += kCompatThreads) {
+      const Rec rc = recs[r];
+      const int j = rc.cell;
+      int ms = -rf + 1, me = rf;
+      if (j + ms < 0) ms = -j;
+      if (j + me > ng) me = ng - j;
+      T E1, E2, val;
+      compat_coefs<T, BOOT>(rc, E1g, E2g, y, n, seed, slab, E1, E2, val);
+      const int lo = max(ms, base - j), hi = min(me, base + tl - j);
+      for (int m = lo; m < hi; ++m) {
+        const int mp = m < 0 ? -m : m;
+        const T e3m = mp < kCompatMaxRf ? e3[mp] : E3g[mp];
+        const T w = val * (E1 * cpow(E2, m) * e3m);
+        FA::add(&acc[j + m - base], FA::to_fix(w * sc));
+      }
     }
   }
   __syncthreads();
   typename CxOf<T>::type *out = f_hat + (int64_t)slab * ng + base;
-  for (int c = threadIdx.x; c < tl; c += blockDim.x) {
-    const T v = acc[c];
-    if (v != (T)0) out[c].x += v;
+  if (isnan(sc)) {  // a non-finite value: the tile is NaN, as the float sums would spread it
+    for (int c = threadIdx.x; c < tl; c += kCompatThreads) out[c].x += (T)NAN;
+    return;
   }
+  const T inv = sc > (T)0 ? (T)1 / sc : (T)0;
+  for (int c = threadIdx.x; c < tl; c += kCompatThreads) {
+    const A v = acc[c];
+    if (v != 0) out[c].x += (T)v * inv;
+  }
+}
+
+template <typename T> constexpr size_t compat_grid_smem() {
+  // accumulators, E3 table, bucket counts (buckets of >= 16 cells)
+  return sizeof(typename FixAcc<T>::type) * (1 << kCompatLogTL) + sizeof(T) * kCompatMaxRf +
+         sizeof(int) * (((1 << kCompatLogTL) + 2 * kCompatMaxRf) / 16 + 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -544,7 +625,7 @@ int compat_grid(const T *x, const T *y, typename CxOf<T>::type *f_hat, int n, in
   if (boot) k_bin_scatter<<<gscat, 512, 2 * smc, st>>>(sb, cw.offsets, cw.cursor, recs, ntiles);
   else k_bin_scatter<<<gscat, 512, 2 * smc, st>>>(sp, cw.offsets, cw.cursor, recs, ntiles);
   CUNA_CK(cudaGetLastError());
-  const size_t smg = sizeof(T) * ((1 << kCompatLogTL) + kCompatMaxRf);
+  const size_t smg = compat_grid_smem<T>();
   if (boot)
     k_grid_compat<T, true><<<dim3(ntiles, nbs), 256, smg, st>>>(recs, cw.offsets, f_hat, ng, dfp, y, n, seed);
   else
@@ -817,7 +898,7 @@ int compat_adjoint_noalloc(const float *x, const float *y, float2 *f_hat, int n,
     CUNA_CK(cudaGetLastError());
     k_bin_scatter<<<gscat, 512, 2 * smc, st>>>(sp, offsets, cursor, recs, ntiles);
     CUNA_CK(cudaGetLastError());
-    const size_t smg = sizeof(float) * ((1 << kCompatLogTL) + kCompatMaxRf);
+    const size_t smg = compat_grid_smem<float>();
     k_grid_compat<float, false><<<dim3(ntiles, 1), 256, smg, st>>>(recs, offsets, f_hat, ng, dfp, y, n, 0u);
     CUNA_CK(cudaGetLastError());
   }
