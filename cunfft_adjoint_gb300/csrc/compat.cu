@@ -565,9 +565,17 @@ int compat_fft(typename CxOf<T>::type *f_hat, int ng, int nbs, const typename Fp
 
 struct CompatWs {
   int *counts, *offsets, *cursor;
+  int *resv;  // reservation table of the two-launch binning (up to kScanFuseTiles tiles)
   void *recs;
   void *scratch;
 };
+
+// blocks of the reserved binning for n samples on ntiles tiles (0: not used)
+inline int compat_resv_blocks(int n, int ntiles) {
+  if (n <= 0 || ntiles > kScanFuseTiles) return 0;
+  const int64_t span = resv_span(n, ntiles);
+  return (int)((n + span - 1) / span);
+}
 
 template <typename T>
 int compat_workspace(int n, int ng, int nbs, bool need_fft, cudaStream_t st, CompatWs *cw) {
@@ -578,7 +586,8 @@ int compat_workspace(int n, int ng, int nbs, bool need_fft, cudaStream_t st, Com
   const bool fourstep = need_fft && pow2 && ilog2i(ng) > (sizeof(T) == 4 ? kSingleLogF32 : kSingleLogF64) &&
                         ilog2i(ng) <= (sizeof(T) == 4 ? 26 : 24);
   const size_t o_off = align_up(sizeof(int) * ntiles), o_cur = o_off + align_up(sizeof(int) * (ntiles + 1));
-  const size_t o_rec = o_cur + align_up(sizeof(int) * ntiles);
+  const size_t o_rsv = o_cur + align_up(sizeof(int) * ntiles);
+  const size_t o_rec = o_rsv + align_up(sizeof(int) * (size_t)compat_resv_blocks(n, ntiles) * ntiles);
   const size_t o_fft = o_rec + align_up(sizeof(Rec) * 2 * (size_t)(n > 0 ? n : 1));
   const size_t bytes = o_fft + (fourstep ? sizeof(C) * (size_t)ng * nbs : 0);
   void *ws = nullptr;
@@ -587,6 +596,7 @@ int compat_workspace(int n, int ng, int nbs, bool need_fft, cudaStream_t st, Com
   cw->counts = (int *)w;
   cw->offsets = (int *)(w + o_off);
   cw->cursor = (int *)(w + o_cur);
+  cw->resv = (int *)(w + o_rsv);
   cw->recs = w + o_rec;
   cw->scratch = fourstep ? (void *)(w + o_fft) : nullptr;
   return CUNA2_SUCCESS;
@@ -617,14 +627,40 @@ int compat_grid(const T *x, const T *y, typename CxOf<T>::type *f_hat, int n, in
   const int gcount = (int)std::min<int64_t>((n + 4095) / 4096, 4 * sms);
   const int gscat = (int)((n + 512 * kScatterItems - 1) / (512 * kScatterItems));
   CUNA_CK(cudaMemsetAsync(cw.counts, 0, sizeof(int) * ntiles, st));
-  if (boot) k_bin_count<<<gcount, 512, smc, st>>>(sb, cw.counts, ntiles);
-  else k_bin_count<<<gcount, 512, smc, st>>>(sp, cw.counts, ntiles);
-  CUNA_CK(cudaGetLastError());
-  k_scan_tiles<<<1, 1024, 0, st>>>(cw.counts, cw.offsets, cw.cursor, ntiles);
-  CUNA_CK(cudaGetLastError());
-  if (boot) k_bin_scatter<<<gscat, 512, 2 * smc, st>>>(sb, cw.offsets, cw.cursor, recs, ntiles);
-  else k_bin_scatter<<<gscat, 512, 2 * smc, st>>>(sp, cw.offsets, cw.cursor, recs, ntiles);
-  CUNA_CK(cudaGetLastError());
+  const int nrb = compat_resv_blocks(n, ntiles);
+  if (nrb > 0) {
+    // count + reserve, then scan + scatter without global atomics (binning.cuh)
+    const int64_t span = resv_span(n, ntiles);
+    const size_t sms3 = sizeof(int) * (3 * (size_t)ntiles + 1);
+    static bool attr = false;
+    if (!attr) {
+      const int mx = (int)(sizeof(int) * (3 * kScanFuseTiles + 1));
+      CUNA_CK(cudaFuncSetAttribute(k_bin_scatter_resv<SampCompat<T, false>>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+      CUNA_CK(cudaFuncSetAttribute(k_bin_scatter_resv<SampCompat<T, true>>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+      attr = true;
+    }
+    if (boot) {
+      k_bin_count_resv<<<nrb, 512, sizeof(int) * ntiles, st>>>(sb, cw.counts, cw.resv, ntiles, span);
+      CUNA_CK(cudaGetLastError());
+      k_bin_scatter_resv<<<nrb, 512, sms3, st>>>(sb, cw.counts, cw.resv, cw.offsets, recs, ntiles, span);
+    } else {
+      k_bin_count_resv<<<nrb, 512, sizeof(int) * ntiles, st>>>(sp, cw.counts, cw.resv, ntiles, span);
+      CUNA_CK(cudaGetLastError());
+      k_bin_scatter_resv<<<nrb, 512, sms3, st>>>(sp, cw.counts, cw.resv, cw.offsets, recs, ntiles, span);
+    }
+    CUNA_CK(cudaGetLastError());
+  } else {
+    if (boot) k_bin_count<<<gcount, 512, smc, st>>>(sb, cw.counts, ntiles);
+    else k_bin_count<<<gcount, 512, smc, st>>>(sp, cw.counts, ntiles);
+    CUNA_CK(cudaGetLastError());
+    k_scan_tiles<<<1, 1024, 0, st>>>(cw.counts, cw.offsets, cw.cursor, ntiles);
+    CUNA_CK(cudaGetLastError());
+    if (boot) k_bin_scatter<<<gscat, 512, 2 * smc, st>>>(sb, cw.offsets, cw.cursor, recs, ntiles);
+    else k_bin_scatter<<<gscat, 512, 2 * smc, st>>>(sp, cw.offsets, cw.cursor, recs, ntiles);
+    CUNA_CK(cudaGetLastError());
+  }
   const size_t smg = compat_grid_smem<T>();
   if (boot)
     k_grid_compat<T, true><<<dim3(ntiles, nbs), 256, smg, st>>>(recs, cw.offsets, f_hat, ng, dfp, y, n, seed);
