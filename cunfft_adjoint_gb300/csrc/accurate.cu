@@ -113,6 +113,23 @@ int plan_workspace(cuna2_plan_st *p, size_t bytes, void **ws) {
   return CUNA2_SUCCESS;
 }
 
+// Launch with programmatic stream serialization: the kernel may start while
+// its predecessor finishes and waits for it with pdl_wait() (common.cuh).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 // Optional per-launch event marks (cuna2_plan_profile).
 struct Prof {
   cudaEvent_t ev[16];
@@ -160,12 +177,14 @@ int ct_passes_at(typename CxOf<T>::type *z, const FftDev<T> &f, const AccParams<
       tma = true;
     }
   }
-  if (!tma)
-    k_ct_colpass<T, LOGL><<<dim3((1 << LOG2) / BA, nslab), PassCfg<T>::THREADS, smA, st>>>(z, f, (int64_t)1 << LOGL);
+  if (!tma && launch_pdl(k_ct_colpass<T, LOGL>, dim3((1 << LOG2) / BA, nslab), dim3(PassCfg<T>::THREADS), smA, st, z,
+                         f, (int64_t)1 << LOGL) != cudaSuccess)
+    return -1;
   if (cudaPeekAtLastError() != cudaSuccess) return -1;
   mark(pr, "fft_colpass", st);
-  k_ct_rowpass_acc<T, LOGL><<<dim3(ct_rowpass_ctas<T, LOGL>(), nslab), PassCfg<T>::THREADS, smB, st>>>(z, f, e, F);
-  if (cudaPeekAtLastError() != cudaSuccess) return -1;
+  if (launch_pdl(k_ct_rowpass_acc<T, LOGL>, dim3(ct_rowpass_ctas<T, LOGL>(), nslab), dim3(PassCfg<T>::THREADS), smB,
+                 st, z, f, e, F) != cudaSuccess)
+    return -1;
   mark(pr, "fft_rowpass", st);
   return 1;
 }
@@ -302,9 +321,8 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     k_bin_count_resv<<<nrb, 512, sizeof(int) * ntiles, st>>>(smp, counts, rsv, ntiles, rspan);
     CUNA_CK(cudaGetLastError());
     mark(pr, "bin_count", st);
-    k_bin_scatter_resv<<<nrb, 512, sizeof(int) * (3 * ntiles + 1), st>>>(sms, counts, rsv, offsets, recs, ntiles,
-                                                                         rspan);
-    CUNA_CK(cudaGetLastError());
+    CUNA_CK(launch_pdl(k_bin_scatter_resv<SampAccS<T>>, dim3(nrb), dim3(512), sizeof(int) * (3 * ntiles + 1), st, sms,
+                       (const int *)counts, (const int *)rsv, offsets, recs, ntiles, rspan));
     mark(pr, "bin_scatter", st);
   } else if (n > 0) {
     SampAcc<T> smp{t, y, n, pm, e};
@@ -367,17 +385,23 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
                                                      p->ng);
     }
   } else {
+    const Rec *rc = recs;
+    const int *oc = offsets;
+    const T *wc = wts;
+    const int64_t nv = n, sstr = p->ng;
+    cudaError_t le;
     if (p->grid_method == CUNA2_GRID_GATHER && cw8 && wts && group >= 2) {
       const size_t sm4 = grid_smem_bytes<T>(p->logTL, p->m, 4);
-      k_grid_acc_sg4<T><<<ggrid, gb, sm4, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+      le = launch_pdl(k_grid_acc_sg4<T>, ggrid, gb, sm4, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
     } else if (p->grid_method == CUNA2_GRID_GATHER) {
-      if (cw8) k_grid_acc<T, 8><<<ggrid, gb, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
-      else k_grid_acc<T, 4><<<ggrid, gb, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+      if (cw8) le = launch_pdl(k_grid_acc<T, 8>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+      else le = launch_pdl(k_grid_acc<T, 4>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
     } else if (p->grid_method == CUNA2_GRID_FIXED) {
-      k_grid_fixed<T><<<ggrid, gb, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+      le = launch_pdl(k_grid_fixed<T>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
     } else {
-      k_grid_scatter<T><<<ggrid, gb, smg, st>>>(recs, offsets, grid, e, wts, n, nslab, group, p->ng);
+      le = launch_pdl(k_grid_scatter<T>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
     }
+    CUNA_CK(le);
   }
   CUNA_CK(cudaGetLastError());
   mark(pr, "grid", st);

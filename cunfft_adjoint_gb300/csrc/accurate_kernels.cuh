@@ -581,6 +581,8 @@ template <typename T>
 __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 3 : 2) k_grid_acc_sg4(
     const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
     AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab, int group, int64_t slab_stride) {
+  pdl_trigger();
+  pdl_wait();  // records and offsets come from the binning
   const int tile = blockIdx.x;
   const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
   const typename RecOf<T>::type *rp = recs;
@@ -596,6 +598,8 @@ template <typename T, int CW>
 __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 4 : 2) k_grid_acc(
     const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
     AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab, int group, int64_t slab_stride) {
+  pdl_trigger();
+  pdl_wait();  // records and offsets come from the binning
   // a CTA per (tile, group of slabs)
   const int tile = blockIdx.x;
   const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
@@ -674,6 +678,8 @@ template <typename T>
 __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 3) k_grid_scatter(
     const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
     AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab, int group, int64_t slab_stride) {
+  pdl_trigger();
+  pdl_wait();  // records and offsets come from the binning
   const int tile = blockIdx.x;
   const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
   grid_tile_scatter<T>(recs, off[tile], off[tile + 1], tile << e.logTL, grid, e, wts, nvals, sbeg, send,
@@ -849,6 +855,8 @@ template <typename T>
 __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 2) k_grid_fixed(
     const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
     AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab, int group, int64_t slab_stride) {
+  pdl_trigger();
+  pdl_wait();  // records and offsets come from the binning
   const int tile = blockIdx.x;
   const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
   grid_tile_fixed<T>(recs, off[tile], off[tile + 1], tile << e.logTL, grid, e, wts, nvals, sbeg, send, slab_stride);

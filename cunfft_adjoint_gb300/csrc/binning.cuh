@@ -224,6 +224,7 @@ __global__ void __launch_bounds__(512) k_bin_count_resv(S smp, int *__restrict__
                                                         int ntiles, int64_t span) {
   extern __shared__ int lc[];
   constexpr int TPT = kScanFuseTiles / 512;
+  pdl_trigger();  // the scatter pass may launch and wait for this grid
 #pragma unroll
   for (int k = 0; k < TPT; ++k) {
     const int t = threadIdx.x + k * 512;
@@ -273,6 +274,8 @@ __global__ void __launch_bounds__(512) k_bin_scatter_resv(S smp, const int *__re
   int *lc = sh, *base = sh + ntiles, *off = sh + 2 * ntiles;  // off: ntiles + 1
   constexpr int TPT = kScanFuseTiles / 512;
   const int *rv = resv + (int64_t)blockIdx.x * ntiles;
+  pdl_trigger();
+  pdl_wait();  // counts and reservations come from the count pass
   int res[TPT];
 #pragma unroll
   for (int k = 0; k < TPT; ++k) {

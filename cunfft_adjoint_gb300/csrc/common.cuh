@@ -56,6 +56,16 @@ __host__ __device__ __forceinline__ int ilog2i(int64_t v) {
   return r;
 }
 
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialization may start while its predecessor in the stream is finishing:
+// pdl_trigger() lets the successor launch once every CTA of this grid has
+// called it, and pdl_wait() blocks until the predecessor grid has completed
+// and its memory is visible (a hardware grid-completion wait; it returns at
+// once when the kernel was launched without the attribute).  Every read of a
+// predecessor's output must follow pdl_wait().
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Fixed-point accumulation in shared memory: a value w (already scaled so
 // that every cell's sum stays within `range`) is rounded to an integer and
 // added with a native shared-memory integer atomic; integer sums do not

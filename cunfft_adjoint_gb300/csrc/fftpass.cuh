@@ -49,12 +49,14 @@ __device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *__
   // behind the FFT buffer: the CTA's 2P rows and all L2 columns
   C *twr = s + PITCH * B, *twc = twr + B;
   const int p0 = pblock * P;
+  pdl_trigger();
   for (int u = threadIdx.x; u < B + L2; u += THREADS) {
     const int q = u < B ? ct_pair_row<LOG1>(p0 + (u >> 1), u & 1) : (u - B) << LOG1;
     T sn, cs;
     sincospi_t((T)q * e.twk, &sn, &cs);
     twr[u] = cmk(cs, sn);  // twr[B + k2] is twc[k2]
   }
+  pdl_wait();  // the rows come from the column pass
   CtPairSrc<T, LOG1, LOG2> src{slab, p0};
   ct_fft<T, LOG2, LOGB, false, false, false>(s, f.tw2, src, CtNoDst());
 #pragma unroll 4

@@ -193,10 +193,12 @@ __device__ __forceinline__ void ct_colpass_body(const typename CxOf<T>::type *in
   C *s = reinterpret_cast<C *>(smem_raw);
   C *steps = s + PITCH * B;
   const int c0 = cblock * B;
+  pdl_trigger();
   // stride 17 so that the columns of one row of the table fall in different banks
   for (int i = threadIdx.x; i < 16 * B; i += PassCfg<T>::THREADS)
     steps[(i >> 4) * 17 + (i & 15)] = twiddle_L(f, (c0 + (i >> 4)) * ((i & 15) << LNS));
   // the steps table is read only by the storing stage, after at least one barrier
+  pdl_wait();  // the grid comes from the gridding
   CtColSrc<T, LOG1, LOG2> src{in + c0};
   CtColDst<T, LOG1, LOG2, LOGB> dst{out + c0, steps, f, c0};
   // reads all precede the first barrier, writes all follow it: in place is safe
