@@ -113,23 +113,6 @@ int plan_workspace(cuna2_plan_st *p, size_t bytes, void **ws) {
   return CUNA2_SUCCESS;
 }
 
-// Launch with programmatic stream serialization: the kernel may start while
-// its predecessor finishes and waits for it with pdl_wait() (common.cuh).
-template <typename... KArgs, typename... Args>
-cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
-}
-
 // Optional per-launch event marks (cuna2_plan_profile).
 struct Prof {
   cudaEvent_t ev[16];
