@@ -241,7 +241,7 @@ template <typename T> struct SampAccS {
   AccParams<T> e;
   __device__ __forceinline__ Raw load(int64_t i, bool with_value) const {
     Raw r;
-    r.S = sc[i];
+    r.S = __ldcg(reinterpret_cast<const unsigned long long *>(sc) + i);  // written by the count pass
     if (with_value) r.y = y[i];
     return r;
   }
@@ -579,32 +579,33 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
 // slab groups sharing each record's Gaussian (bootstrap resamples, channels)
 template <typename T>
 __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 3 : 2) k_grid_acc_sg4(
-    const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
-    AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab, int group, int64_t slab_stride) {
+    const typename RecOf<T>::type *recs, const int *off, T *grid, AccParams<T> e, const T *wts, int64_t nvals,
+    int nslab, int group, int64_t slab_stride) {
   pdl_trigger();
   pdl_wait();  // records and offsets come from the binning
   const int tile = blockIdx.x;
   const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
-  const typename RecOf<T>::type *rp = recs;
+  const CgSrc<typename RecOf<T>::type> rp{recs};
+  const int r0 = __ldcg(off + tile), r1 = __ldcg(off + tile + 1);
   if constexpr (sizeof(T) == 4)
-    grid_tile_body<T, 8, const typename RecOf<T>::type *, 4>(rp, off[tile], off[tile + 1], tile << e.logTL, grid, e,
-                                                              wts, nvals, sbeg, send, slab_stride);
+    grid_tile_body<T, 8, CgSrc<typename RecOf<T>::type>, 4>(rp, r0, r1, tile << e.logTL, grid, e, wts, nvals, sbeg,
+                                                             send, slab_stride);
   else  // double plans keep one slab per pass (four accumulator sets do not fit)
-    grid_tile_body<T, 8>(rp, off[tile], off[tile + 1], tile << e.logTL, grid, e, wts, nvals, sbeg, send,
-                         slab_stride);
+    grid_tile_body<T, 8>(rp, r0, r1, tile << e.logTL, grid, e, wts, nvals, sbeg, send, slab_stride);
 }
 
 template <typename T, int CW>
 __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 4 : 2) k_grid_acc(
-    const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
-    AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab, int group, int64_t slab_stride) {
+    const typename RecOf<T>::type *recs, const int *off, T *grid, AccParams<T> e, const T *wts, int64_t nvals,
+    int nslab, int group, int64_t slab_stride) {
   pdl_trigger();
   pdl_wait();  // records and offsets come from the binning
   // a CTA per (tile, group of slabs)
   const int tile = blockIdx.x;
   const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
-  grid_tile_body<T, CW>(recs, off[tile], off[tile + 1], tile << e.logTL, grid, e, wts, nvals, sbeg, send,
-                        slab_stride);
+  const CgSrc<typename RecOf<T>::type> rp{recs};
+  grid_tile_body<T, CW>(rp, __ldcg(off + tile), __ldcg(off + tile + 1), tile << e.logTL, grid, e, wts, nvals, sbeg,
+                        send, slab_stride);
 }
 
 // Scatter form of the same tile gridding: the tile's cells accumulate in
@@ -676,14 +677,15 @@ __device__ __forceinline__ void grid_tile_scatter(const Src &recs, int r0, int r
 
 template <typename T>
 __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 3) k_grid_scatter(
-    const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
-    AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab, int group, int64_t slab_stride) {
+    const typename RecOf<T>::type *recs, const int *off, T *grid, AccParams<T> e, const T *wts, int64_t nvals,
+    int nslab, int group, int64_t slab_stride) {
   pdl_trigger();
   pdl_wait();  // records and offsets come from the binning
   const int tile = blockIdx.x;
   const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
-  grid_tile_scatter<T>(recs, off[tile], off[tile + 1], tile << e.logTL, grid, e, wts, nvals, sbeg, send,
-                       slab_stride);
+  const CgSrc<typename RecOf<T>::type> rp{recs};
+  grid_tile_scatter<T>(rp, __ldcg(off + tile), __ldcg(off + tile + 1), tile << e.logTL, grid, e, wts, nvals, sbeg,
+                       send, slab_stride);
 }
 
 // Fixed-point form: one thread per record, all 2m taps from the fast Gaussian
@@ -853,13 +855,15 @@ __device__ __forceinline__ void grid_tile_fixed(const Src &recs, int r0, int r1,
 
 template <typename T>
 __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 2) k_grid_fixed(
-    const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
-    AccParams<T> e, const T *__restrict__ wts, int64_t nvals, int nslab, int group, int64_t slab_stride) {
+    const typename RecOf<T>::type *recs, const int *off, T *grid, AccParams<T> e, const T *wts, int64_t nvals,
+    int nslab, int group, int64_t slab_stride) {
   pdl_trigger();
   pdl_wait();  // records and offsets come from the binning
   const int tile = blockIdx.x;
   const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
-  grid_tile_fixed<T>(recs, off[tile], off[tile + 1], tile << e.logTL, grid, e, wts, nvals, sbeg, send, slab_stride);
+  const CgSrc<typename RecOf<T>::type> rp{recs};
+  grid_tile_fixed<T>(rp, __ldcg(off + tile), __ldcg(off + tile + 1), tile << e.logTL, grid, e, wts, nvals, sbeg, send,
+                     slab_stride);
 }
 
 template <typename T> size_t grid_fixed_smem_bytes(int logTL, int m) {

@@ -265,10 +265,8 @@ __global__ void __launch_bounds__(512) k_bin_count_resv(S smp, int *__restrict__
 }
 
 template <class S>
-__global__ void __launch_bounds__(512) k_bin_scatter_resv(S smp, const int *__restrict__ counts,
-                                                          const int *__restrict__ resv, int *__restrict__ offsets,
-                                                          typename S::Rec *__restrict__ recs, int ntiles,
-                                                          int64_t span) {
+__global__ void __launch_bounds__(512) k_bin_scatter_resv(S smp, const int *counts, const int *resv, int *offsets,
+                                                          typename S::Rec *recs, int ntiles, int64_t span) {
   typedef typename S::Rec Rec;
   extern __shared__ int sh[];
   int *lc = sh, *base = sh + ntiles, *off = sh + 2 * ntiles;  // off: ntiles + 1
@@ -283,8 +281,8 @@ __global__ void __launch_bounds__(512) k_bin_scatter_resv(S smp, const int *__re
     res[k] = 0;
     if (t < ntiles) {
       lc[t] = 0;
-      base[t] = counts[t];
-      res[k] = rv[t];  // entries of untouched tiles are stale and never used
+      base[t] = __ldcg(counts + t);  // the count pass's output, through L2
+      res[k] = __ldcg(rv + t);       // entries of untouched tiles are stale and never used
     }
   }
   __syncthreads();

@@ -50,6 +50,22 @@ template <typename T> struct RecOf;
 template <> struct RecOf<float> { typedef RecF type; };
 template <> struct RecOf<double> { typedef RecD type; };
 
+// Records read through L2 only (ld.global.cg), for kernels that start before
+// the kernel writing the records has finished (dependent launch): no L1 line
+// filled before the grid-completion wait can serve them.
+template <typename R> struct CgSrc {
+  const R *p;
+  __device__ __forceinline__ R operator[](int64_t i) const {
+    static_assert(sizeof(R) % 16 == 0, "records are whole 16-byte vectors");
+    R r;
+    const int4 *s = reinterpret_cast<const int4 *>(p + i);
+    int4 *d = reinterpret_cast<int4 *>(&r);
+#pragma unroll
+    for (int q = 0; q < (int)(sizeof(R) / 16); ++q) d[q] = __ldcg(s + q);
+    return r;
+  }
+};
+
 __host__ __device__ __forceinline__ int ilog2i(int64_t v) {
   int r = 0;
   while ((int64_t(1) << (r + 1)) <= v) ++r;
@@ -62,14 +78,27 @@ __host__ __device__ __forceinline__ int ilog2i(int64_t v) {
 // called it, and pdl_wait() blocks until the predecessor grid has completed
 // and its memory is visible (a hardware grid-completion wait; it returns at
 // once when the kernel was launched without the attribute).  Every read of a
-// predecessor's output must follow pdl_wait().
+// predecessor's output must follow pdl_wait() and be an ordinary (coherent)
+// load: no __ldg on it and no __restrict__ parameter in the kernel (from
+// restrict-qualified outputs the compiler may infer that the other inputs are
+// read-only and read them through the non-coherent path).  Non-coherent loads
+// assume the data does not change while the kernel runs, and here the kernel
+// starts before its predecessors have finished writing (measured: a row pass
+// reading the column pass's output through const __restrict__ returned a
+// wrong spectrum whenever it ran one CTA per SM).
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // Launch with programmatic stream serialization: the kernel may start while
 // its predecessor finishes and waits for it with pdl_wait() (common.cuh).
+bool pdl_enabled();  // runtime.cu: false when the environment sets CUNA2_PDL=0
+
 template <typename... KArgs, typename... Args>
 cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+  if (!pdl_enabled()) {
+    k<<<grid, block, smem, st>>>(static_cast<KArgs>(args)...);
+    return cudaGetLastError();
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;

@@ -24,7 +24,8 @@ template <typename T, int LOG1, int LOG2> struct CtPairSrc {
   const typename CxOf<T>::type *p;  // slab
   int p0;
   __device__ __forceinline__ typename CxOf<T>::type load(int seq, int j, int dr) const {
-    return p[(ct_pair_row<LOG1>(p0 + (seq >> 1), seq & 1) << LOG2) + j + dr];
+    // through L2: the column pass may still have been writing when this kernel started
+    return __ldcg(p + (ct_pair_row<LOG1>(p0 + (seq >> 1), seq & 1) << LOG2) + j + dr);
   }
 };
 
@@ -34,7 +35,7 @@ struct CtNoDst {
 
 // row-pair block `pblock` of one packed grid z; outputs Fs[0 .. nf)
 template <typename T, int LOGL>
-__device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *__restrict__ slab, const FftDev<T> &f,
+__device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *slab, const FftDev<T> &f,
                                                 const AccParams<T> &e, typename CxOf<T>::type *Fs, int pblock) {
   typedef typename CxOf<T>::type C;
   constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
@@ -76,8 +77,10 @@ __device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *__
   }
 }
 
+// three CTAs per SM for the short rows of many small grids (bootstrap), where
+// the pass streams from HBM and more bytes in flight pay
 template <typename T, int LOGL>
-__global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_rowpass_acc(const typename CxOf<T>::type *__restrict__ grid,
+__global__ void __launch_bounds__(PassCfg<T>::THREADS, (sizeof(T) == 4 && LOGL <= 15) ? 3 : 2) k_ct_rowpass_acc(const typename CxOf<T>::type *grid,
                                                                         FftDev<T> f, AccParams<T> e,
                                                                         typename CxOf<T>::type *F) {
   ct_rowpass_body<T, LOGL>(grid + ((int64_t)blockIdx.y << LOGL), f, e, F + (int64_t)blockIdx.y * e.nf, blockIdx.x);

@@ -150,7 +150,8 @@ __device__ __forceinline__ void ct_fft(typename CxOf<T>::type *s, const typename
 template <typename T, int LOG1, int LOG2> struct CtColSrc {
   const typename CxOf<T>::type *p;  // slab + c0
   __device__ __forceinline__ typename CxOf<T>::type load(int seq, int j, int dr) const {
-    return p[((j + dr) << LOG2) + seq];
+    // through L2: the gridding may still have been writing when this kernel started
+    return __ldcg(p + ((j + dr) << LOG2) + seq);
   }
 };
 

@@ -203,6 +203,14 @@ int *wait_timeout_counter() {
   return g_timeouts_dev;
 }
 
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char *v = getenv("CUNA2_PDL");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
 bool tma_enabled() {
   static const bool on = [] {
     const char *v = getenv("CUNA2_TMA");
