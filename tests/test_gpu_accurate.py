@@ -337,41 +337,59 @@ def test_plan_for_tolerance(nfft, oracle_lib, dtype, tol):
     assert rel_l2(F[k + nf // 2], D) < tol
 
 
-_TMA_SCRIPT = r"""
+_SWITCH_SCRIPT = r"""
 import sys, numpy as np, torch
 sys.path.insert(0, sys.argv[1])
 from cunfft_adjoint_gb300 import nfft as N, _lib
 out = {}
-for nf, R in [(1 << 15, 2), (1 << 15, 4), (1 << 17, 2), (1 << 17, 4), (1 << 19, 2), (1 << 19, 4),
-              (1 << 21, 2), (1 << 21, 4), (1 << 23, 2), (1 << 23, 4)]:
+cases = [(nf, R, torch.float32) for nf in (1 << 13, 1 << 15, 1 << 17, 1 << 19, 1 << 21, 1 << 23) for R in (2, 4)]
+if sys.argv[3] == "all":
+    cases += [(nf, R, torch.float64) for nf in (1 << 12, 1 << 15, 1 << 18, 1 << 21) for R in (2, 4)]
+for nf, R, dt in cases:
     rng = np.random.default_rng(nf + R)
     t = torch.as_tensor(rng.uniform(0, 100.0, 50_000), device="cuda")
-    y = torch.as_tensor(rng.normal(0, 1, 50_000), dtype=torch.float32, device="cuda")
-    plan = N.AdjointNFFT(nf, R, 8, torch.float32)
+    y = torch.as_tensor(rng.normal(0, 1, 50_000), dtype=dt, device="cuda")
+    plan = N.AdjointNFFT(nf, R, 8, dt)
     plan.set_schedule(12, _lib.GRID_FIXED)
-    out["%d_%d" % (nf, R)] = plan(t, y, 0.0, 100.0).cpu().numpy()
+    for rep in range(2):
+        out["%d_%d_%s_%d" % (nf, R, str(dt)[-7:], rep)] = plan(t, y, 0.0, 100.0).cpu().numpy()
 np.savez(sys.argv[2], **out)
 print(_lib.core().cuna2_wait_timeouts())
 """
 
 
-def test_tma_column_pass_matches_plain(tmp_path):
-    """The opt-in TMA column pass (CUNA2_TMA=1) stages its columns through
-    tensor-map boxes (packed lengths 2^15 .. 2^24 here); with fixed-point
-    gridding (identical grids) its spectra are bit-identical to the default
-    load/store column pass, and no bounded wait ran out."""
+def _spectra_under(tmp_path, tag, env, which):
     import os
     import subprocess
     import sys
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    script = tmp_path / "tma.py"
-    script.write_text(_TMA_SCRIPT)
-    res = {}
-    for tag, env in (("tma", {"CUNA2_TMA": "1"}), ("plain", {"CUNA2_TMA": "0"})):
-        out = subprocess.run([sys.executable, str(script), root, str(tmp_path / (tag + ".npz"))],
-                             env={**os.environ, **env}, capture_output=True, text=True, timeout=600)
-        assert out.returncode == 0, out.stderr[-2000:]
-        assert out.stdout.strip().splitlines()[-1] == "0"
-        res[tag] = np.load(tmp_path / (tag + ".npz"))
-    for key in res["tma"].files:
-        assert np.array_equal(res["tma"][key], res["plain"][key]), key
+    script = tmp_path / "switch.py"
+    script.write_text(_SWITCH_SCRIPT)
+    out = subprocess.run([sys.executable, str(script), root, str(tmp_path / (tag + ".npz")), which],
+                         env={**os.environ, **env}, capture_output=True, text=True, timeout=900)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.strip().splitlines()[-1] == "0"
+    return np.load(tmp_path / (tag + ".npz"))
+
+
+def test_tma_column_pass_matches_plain(tmp_path):
+    """The opt-in TMA column pass (CUNA2_TMA=1) stages its columns through
+    tensor-map boxes (float packed lengths 2^13 .. 2^24 here); with
+    fixed-point gridding (identical grids) its spectra are bit-identical to
+    the default load/store column pass, and no bounded wait ran out."""
+    a = _spectra_under(tmp_path, "tma", {"CUNA2_TMA": "1", "CUNA2_PDL": "0"}, "float")
+    b = _spectra_under(tmp_path, "plain", {"CUNA2_TMA": "0", "CUNA2_PDL": "0"}, "float")
+    for key in a.files:
+        assert np.array_equal(a[key], b[key]), key
+
+
+def test_dependent_launch_matches_serial(tmp_path):
+    """Programmatic dependent launch (the default) lets each kernel of a
+    transform start before its predecessor has finished; every float and
+    double length with compile-time passes gives spectra bit-identical to
+    fully serialised launches (CUNA2_PDL=0), twice in a row per plan (fixed-
+    point gridding, so the grids are identical)."""
+    a = _spectra_under(tmp_path, "pdl", {"CUNA2_PDL": "1"}, "all")
+    b = _spectra_under(tmp_path, "serial", {"CUNA2_PDL": "0"}, "all")
+    for key in a.files:
+        assert np.array_equal(a[key], b[key]), key
