@@ -17,6 +17,7 @@
 //
 // With cuna2_batch_set_graph the launch sequence is captured once per
 // argument set and replayed as one CUDA graph.
+#include <limits.h>
 #include <algorithm>
 #include <map>
 #include <mutex>
@@ -40,15 +41,20 @@ template <typename T> struct BDesc {
 struct Item {
   int s;     // series
   int a, b;  // sample range [a, b) (binning) or block index a (FFT passes)
-  int pad;
+  int r;     // binning: start of this block's row of the reservation table
 };
 
 constexpr int kBChunk = 2048;  // samples per binning CTA (512 threads x 4)
 
+// Binning of the large series, in two launches with the reservations of
+// binning.cuh: k_bcount histograms its block of samples per tile and reserves
+// the block's range inside every touched tile (resv[it.r + u], relative to
+// the tile's start); k_bscatter ranks the same samples with shared atomics
+// and writes each record to offsets[tile] + reservation + rank.
 template <typename T>
 __global__ void __launch_bounds__(512) k_bcount(const double *__restrict__ t, const T *__restrict__ y,
                                                 const BDesc<T> *__restrict__ D, const Item *__restrict__ items,
-                                                int *__restrict__ counts) {
+                                                int *__restrict__ counts, int *__restrict__ resv) {
   extern __shared__ int lc[];
   const Item it = items[blockIdx.x];
   const BDesc<T> d = D[it.s];
@@ -71,44 +77,43 @@ __global__ void __launch_bounds__(512) k_bcount(const double *__restrict__ t, co
   }
   __syncthreads();
   for (int u = threadIdx.x; u < d.ntiles; u += blockDim.x)
-    if (lc[u]) atomicAdd(&counts[d.tile0 + u], lc[u]);
+    if (lc[u]) resv[it.r + u] = atomicAdd(&counts[d.tile0 + u], lc[u]);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(512) k_bscatter(const double *__restrict__ t, const T *__restrict__ y,
                                                   const BDesc<T> *__restrict__ D, const Item *__restrict__ items,
-                                                  const int *__restrict__ offsets, int *__restrict__ cursor,
+                                                  const int *__restrict__ offsets, const int *__restrict__ resv,
                                                   typename RecOf<T>::type *__restrict__ recs) {
   typedef typename RecOf<T>::type Rec;
   extern __shared__ int sh[];
   const Item it = items[blockIdx.x];
   const BDesc<T> d = D[it.s];
   int *lc = sh, *lbase = sh + d.ntiles;
-  for (int u = threadIdx.x; u < d.ntiles; u += blockDim.x) lc[u] = 0;
-  __syncthreads();
   SampAcc<T> smp{t + d.s_off, y + d.s_off, d.n, d.pm, d.e};
   typename SampAcc<T>::Raw raw[4];
-  Prep<Rec> p[4];
-  int rk[4][2];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int i = it.a + threadIdx.x + k * blockDim.x;
     if (i < it.b) raw[k] = smp.load(i, true);
   }
+  // entries of tiles this block does not touch are stale and never used
+  for (int u = threadIdx.x; u < d.ntiles; u += blockDim.x) {
+    lc[u] = 0;
+    lbase[u] = offsets[d.tile0 + u] + resv[it.r + u];
+  }
+  __syncthreads();
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int i = it.a + threadIdx.x + k * blockDim.x;
-    p[k].nt = 0;
-    if (i < it.b) smp.prep(i, raw[k], p[k]);
-    for (int q = 0; q < p[k].nt; ++q) rk[k][q] = atomicAdd(&lc[p[k].t[q]], 1);
+    if (i >= it.b) continue;
+    Prep<Rec> p;
+    smp.prep(i, raw[k], p);
+    for (int q = 0; q < p.nt; ++q) {
+      const int u = p.t[q];
+      recs[lbase[u] + atomicAdd(&lc[u], 1)] = p.rec;
+    }
   }
-  __syncthreads();
-  for (int u = threadIdx.x; u < d.ntiles; u += blockDim.x)
-    if (lc[u]) lbase[u] = offsets[d.tile0 + u] + atomicAdd(&cursor[d.tile0 + u], lc[u]);
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-    for (int q = 0; q < p[k].nt; ++q) recs[lbase[p[k].t[q]] + rk[k][q]] = p[k].rec;
 }
 
 template <typename T>
@@ -279,6 +284,7 @@ struct cuna2_batch_plan_st {
   // workspace
   void *ws = nullptr;
   int *counts = nullptr, *offsets = nullptr, *cursor = nullptr, *scan_totals = nullptr;
+  int *resv = nullptr;  // reservation table of the binning, one row of ntiles per count block
   void *recs = nullptr, *grid = nullptr;
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -304,6 +310,7 @@ template <typename T> int batch_build(cuna2_batch_plan_st *p) {
   std::vector<BDesc<T>> desc(p->nseries);
   std::vector<Item> count_items, col_items, row_items;
   std::vector<int> tile_series;
+  int64_t resv_total = 0;  // entries of the binning's reservation table
   std::map<int, std::vector<int>> small;  // logL -> series
   std::map<int, std::vector<int>> large;  // logL -> series
   int64_t s_off = 0, f_off = 0, g_off = 0;
@@ -336,7 +343,10 @@ template <typename T> int batch_build(cuna2_batch_plan_st *p) {
                     (long long)ng);
       p->max_large_tiles = std::max(p->max_large_tiles, d.ntiles);
       for (int u = 0; u < d.ntiles; ++u) tile_series.push_back(s);
-      for (int64_t a = 0; a < d.n; a += kBChunk) count_items.push_back({s, (int)a, (int)std::min<int64_t>(d.n, a + kBChunk), 0});
+      for (int64_t a = 0; a < d.n; a += kBChunk) {
+        count_items.push_back({s, (int)a, (int)std::min<int64_t>(d.n, a + kBChunk), (int)resv_total});
+        resv_total += d.ntiles;
+      }
       const int L1 = 1 << g.logL1, L2 = 1 << g.logL2;
       const int BA = elems / L1, BB = elems / L2, PB = BB / 2, npairs = L1 / 2 + 1;
       for (int cb = 0; cb < L2 / BA; ++cb) col_items.push_back({s, cb, 0, 0});
@@ -385,11 +395,14 @@ template <typename T> int batch_build(cuna2_batch_plan_st *p) {
   CUNA_TRY(upload(col_items, &p->d_col_items));
   CUNA_TRY(upload(row_items, &p->d_row_items));
   CUNA_TRY(upload(small_list, &p->d_small_list));
-  // workspace: counts | offsets | cursor | scan totals | records | grid
+  if (resv_total > INT_MAX)
+    return fail(CUNA2_ERROR_UNSUPPORTED, "batch too large: %lld binning reservations", (long long)resv_total);
+  // workspace: counts | offsets | cursor | scan totals | reservations | records | grid
   const size_t nt = (size_t)std::max(1, p->tiles_total);
   const size_t o_off = align_up(sizeof(int) * nt), o_cur = o_off + align_up(sizeof(int) * (nt + 1));
   const size_t o_tot = o_cur + align_up(sizeof(int) * nt);
-  const size_t o_rec = o_tot + align_up(sizeof(int) * (nt / kScanChunk + 1));
+  const size_t o_rsv = o_tot + align_up(sizeof(int) * (nt / kScanChunk + 1));
+  const size_t o_rec = o_rsv + align_up(sizeof(int) * (size_t)std::max<int64_t>(1, resv_total));
   const size_t o_grid = o_rec + align_up(sizeof(Rec) * 2 * (size_t)std::max<int64_t>(1, p->large_samples));
   const size_t bytes = o_grid + sizeof(T) * (size_t)std::max<int64_t>(1, p->grid_total);
   cudaError_t e = cudaMalloc(&p->ws, bytes);
@@ -399,6 +412,7 @@ template <typename T> int batch_build(cuna2_batch_plan_st *p) {
   p->offsets = (int *)(w + o_off);
   p->cursor = (int *)(w + o_cur);
   p->scan_totals = (int *)(w + o_tot);
+  p->resv = (int *)(w + o_rsv);
   p->recs = w + o_rec;
   p->grid = w + o_grid;
   CUNA_CK(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
@@ -439,7 +453,8 @@ int batch_run(cuna2_batch_plan_st *p, const double *t, const T *y, typename CxOf
     const int ntl = p->tiles_total;
     CUNA_CK(cudaMemsetAsync(p->counts, 0, sizeof(int) * ntl, st));
     if (p->n_count_items > 0) {
-      k_bcount<T><<<p->n_count_items, 512, p->smem_bin / 2, st>>>(t, y, D, (const Item *)p->d_count_items, p->counts);
+      k_bcount<T><<<p->n_count_items, 512, p->smem_bin / 2, st>>>(t, y, D, (const Item *)p->d_count_items, p->counts,
+                                                                 p->resv);
       CUNA_CK(cudaGetLastError());
     }
     if (ntl <= 2 * kScanChunk) {
@@ -454,7 +469,7 @@ int batch_run(cuna2_batch_plan_st *p, const double *t, const T *y, typename CxOf
     CUNA_CK(cudaGetLastError());
     if (p->n_count_items > 0) {
       k_bscatter<T><<<p->n_count_items, 512, p->smem_bin, st>>>(t, y, D, (const Item *)p->d_count_items, p->offsets,
-                                                               p->cursor, (Rec *)p->recs);
+                                                               p->resv, (Rec *)p->recs);
       CUNA_CK(cudaGetLastError());
     }
     const size_t smg = grid_fixed_smem_bytes<T>(12, p->m);
