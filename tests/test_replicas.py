@@ -58,3 +58,28 @@ def test_reference_arm_only_on_rank_zero(monkeypatch, capsys):
     args = types.SimpleNamespace(gpus=2, steps=5, warmup=3)
     assert bench.reference_arm(args, bench.WORKLOADS["plain"]) is None
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_line_has_contract_keys(monkeypatch, capsys):
+    """Rank 0 of `bench.py --impl reference` prints one JSON line with the
+    contract's keys: the reference's CPU pipeline (the oracle's restatement)
+    timed on the host, its cpu_baseline description and an e2e object
+    without device copies, on the plain workload (N = 1e4, a few seconds)."""
+    import json
+    import bench
+    monkeypatch.setenv("RANK", "0")
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    args = types.SimpleNamespace(gpus=1, steps=3, warmup=1)
+    bench.reference_arm(args, bench.WORKLOADS["plain"])
+    out = [l for l in capsys.readouterr().out.splitlines() if l.startswith("{")]
+    assert len(out) == 1
+    line = json.loads(out[0])
+    for key in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["value"] > 0
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
