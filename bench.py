@@ -309,7 +309,46 @@ def cpu_baseline(wl, budget_s=20.0):
     return {"value": done / el, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
             "sample": "%d transforms of the workload (N=%d, ng=%d, reference compat math, float) "
                       "by the oracle's multi-threaded CPU pipeline" % (done, n, ng),
-            "seconds": round(el, 3)}
+            "seconds": round(el, 3), "beside": cpu_beside(wl, t, ys[0])}
+
+
+def cpu_beside(wl, t, y, budget_s=1.5):
+    """Rows reported beside the CPU baseline, each a bounded sample on the
+    same host cores: the CPU pipeline on the plain (N = 1e4, ng = 32768) and
+    bootstrap-resample (N = 5000, ng = 65536) shapes, the FP64 direct NDFT of
+    the large workload (256 frequencies, rate extrapolated to all Nf) and
+    scipy's FFT of the large grid as a cross-check of the FFT share."""
+    from oracle import oracle
+    out = {}
+
+    def rate(fn):
+        fn()
+        done, t0 = 0, time.perf_counter()
+        while True:
+            fn()
+            done += 1
+            el = time.perf_counter() - t0
+            if el > budget_s or done >= 200:
+                return done / el
+
+    rng = np.random.default_rng(5)
+    for tag, n, ng in (("plain_nfft_per_s", 10_000, 32768), ("bootstrap_resamples_per_s", 5000, 65536)):
+        x = rng.uniform(-0.5, 0.5, n).astype(np.float32)
+        v = rng.normal(0, 1, n).astype(np.float32)
+        p = oracle.CpuPipeline(n, ng)
+        out[tag] = rate(lambda: p.run(x, v))
+    k = np.arange(-128, 128)
+    t0 = time.perf_counter()
+    oracle.ndft(t, y, 0.0, wl["T"], k)
+    el = time.perf_counter() - t0
+    out["ndft_fp64_seconds_per_transform"] = el * wl["nf"] / len(k)
+    try:
+        import scipy.fft
+        g = (rng.normal(size=wl["R"] * wl["nf"]) + 0j).astype(np.complex64)
+        out["scipy_fft_ms"] = 1000.0 / rate(lambda: scipy.fft.ifft(g, workers=oracle.num_threads()))
+    except ImportError:
+        out["scipy_fft_ms"] = None
+    return out
 
 
 def dist_setup(backend):
