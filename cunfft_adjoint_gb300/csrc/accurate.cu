@@ -232,7 +232,7 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   const bool seg = nch > 0;
   // reserved two-pass binning: CTAs of rspan samples, a table of nrb x ntiles
   const bool resv = !small && !seg && n > 0 && ntiles <= kScanFuseTiles;
-  const int64_t rspan = resv ? resv_span(n, ntiles) : 0;
+  const int64_t rspan = resv ? resv_span(n, ntiles, nsm) : 0;
   const int nrb = resv ? (int)((n + rspan - 1) / rspan) : 0;
   // workspace: counts | cursor | offsets | phases or chunk table | reservations
   //            | records | grid slabs | weights

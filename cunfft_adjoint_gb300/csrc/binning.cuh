@@ -215,7 +215,7 @@ __device__ __forceinline__ void cta_exclusive_scan(const int *in, int *out, int 
 // The ranks of CTA b in the second pass cover exactly the counts it reserved
 // in the first, so the positions are a permutation of [0, offsets[ntiles]).
 // No global atomic is left in the scatter pass and nothing waits on one.
-// Both are launched with 512 threads; span is a multiple of 512*kCountItems.
+// Both are launched with 512 threads; span is a multiple of 512.
 constexpr int kScanFuseTiles = 4096;  // 3 shared arrays of ntiles ints: 48 KB
 constexpr int kResvEntries = 1 << 22; // reservation table limit (ints)
 
@@ -317,14 +317,14 @@ __global__ void __launch_bounds__(512) k_bin_scatter_resv(S smp, const int *coun
   }
 }
 
-// Samples per CTA of the reserved binning: at least 512*kCountItems, and
+// Samples per CTA of the reserved binning: about two CTAs per SM (nsm SMs)
+// so that the one wave is balanced, a multiple of 512, at least 512, and
 // enough that the reservation table (CTAs x ntiles ints) stays within
 // kResvEntries.
-inline int64_t resv_span(int64_t n, int ntiles) {
-  const int64_t unit = 512 * kCountItems;
+inline int64_t resv_span(int64_t n, int ntiles, int nsm) {
   const int64_t maxb = std::max<int64_t>(1, kResvEntries / std::max(ntiles, 1));
-  int64_t span = (n + maxb - 1) / maxb;
-  span = std::max(unit, (span + unit - 1) / unit * unit);
+  int64_t span = std::max((n + maxb - 1) / maxb, (n + 2 * (int64_t)nsm - 1) / (2 * (int64_t)std::max(nsm, 1)));
+  span = std::max<int64_t>(512, (span + 511) / 512 * 512);
   return span;
 }
 

@@ -573,7 +573,7 @@ struct CompatWs {
 // blocks of the reserved binning for n samples on ntiles tiles (0: not used)
 inline int compat_resv_blocks(int n, int ntiles) {
   if (n <= 0 || ntiles > kScanFuseTiles) return 0;
-  const int64_t span = resv_span(n, ntiles);
+  const int64_t span = resv_span(n, ntiles, device_sm_count());
   return (int)((n + span - 1) / span);
 }
 
@@ -630,7 +630,7 @@ int compat_grid(const T *x, const T *y, typename CxOf<T>::type *f_hat, int n, in
   const int nrb = compat_resv_blocks(n, ntiles);
   if (nrb > 0) {
     // count + reserve, then scan + scatter without global atomics (binning.cuh)
-    const int64_t span = resv_span(n, ntiles);
+    const int64_t span = resv_span(n, ntiles, device_sm_count());
     const size_t sms3 = sizeof(int) * (3 * (size_t)ntiles + 1);
     static bool attr = false;
     if (!attr) {

@@ -275,8 +275,8 @@ def test_host_async_two_streams(nfft):
 
 def test_reserved_binning_many_blocks(nfft, oracle_lib):
     """10,000,001 unsorted samples on 2048 tiles: the two-launch reserved
-    binning runs each block over two sub-chunks of 4096 samples (its
-    reservation table holds 2^22 entries) with a ragged last block; the
+    binning runs each block over several sub-chunks of 4096 samples and a
+    partial one, with a ragged last block; the
     spectrum equals the one binned by the three-launch form (8192 tiles,
     more than the fused scan takes) and the NDFT."""
     from cunfft_adjoint_gb300 import _lib
