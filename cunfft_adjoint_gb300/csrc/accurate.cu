@@ -135,12 +135,12 @@ int ct_passes_at(typename CxOf<T>::type *z, const FftDev<T> &f, const AccParams<
   constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
   constexpr int BA = PassCfg<T>::ELEMS >> LOG1;
   constexpr size_t smA = ct_colpass_smem<T, LOGL>(), smB = ct_rowpass_smem<T, LOGL>();
-  static bool attr = false;
-  if (!attr) {
+  static char attr;
+  if (!setup_done(&attr)) {
     if (cudaFuncSetAttribute(k_ct_colpass<T, LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smA) ||
         cudaFuncSetAttribute(k_ct_rowpass_acc<T, LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smB))
       return -1;
-    attr = true;
+    mark_setup_done(&attr);
   }
   bool tma = false;
   if constexpr (sizeof(T) == 4 && TmaCol<LOGL>::ok) {
@@ -148,12 +148,12 @@ int ct_passes_at(typename CxOf<T>::type *z, const FftDev<T> &f, const AccParams<
     int *tmo = tma_enabled() ? wait_timeout_counter() : nullptr;
     alignas(64) CUtensorMap map;
     if (tmo && ct_colpass_tma_map<LOGL>(&map, z, nslab)) {
-      static bool attr_tma = false;
-      if (!attr_tma) {
+      static char attr_tma;
+      if (!setup_done(&attr_tma)) {
         if (cudaFuncSetAttribute(k_ct_colpass_tma<LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)ct_colpass_tma_smem<LOGL>()))
           return -1;
-        attr_tma = true;
+        mark_setup_done(&attr_tma);
       }
       k_ct_colpass_tma<LOGL><<<dim3((1 << LOG2) / BA, nslab), PassCfg<T>::THREADS, ct_colpass_tma_smem<LOGL>(), st>>>(
           map, f, tmo);
@@ -258,11 +258,11 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   T *wts = multi ? const_cast<T *>(multi) : (nbs > 0 ? (T *)(w + o_wts) : nullptr);
   mark(pr, "start", st);
   if (nbs > 0) {
-    static bool attrw = false;
-    if (!attrw) {
+    static char attrw;
+    if (!setup_done(&attrw)) {
       CUNA_CK(cudaFuncSetAttribute(k_boot_weights<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)(sizeof(int) * kBootSmemN)));
-      attrw = true;
+      mark_setup_done(&attrw);
     }
     const bool sm = n <= kBootSmemN;
     if (!sm) CUNA_CK(cudaMemsetAsync(wts, 0, sizeof(T) * (size_t)n * nbs, st));
@@ -271,10 +271,10 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     mark(pr, "boot_weights", st);
   }
   if (small) {
-    static bool attr = false;
-    if (!attr) {
+    static char attr;
+    if (!setup_done(&attr)) {
       CUNA_CK(cudaFuncSetAttribute(k_nfft_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-      attr = true;
+      mark_setup_done(&attr);
     }
     const size_t smem = sizeof(C) * (size_t)fft_pitch(L, 1) + sizeof(T) * (2 * p->m + 2);
     const int threads = std::max(32, std::min(1024, L / kFftE));
@@ -295,11 +295,11 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     // count (caching each sample's phase) and reserve, then scan + scatter
     SampAcc<T> smp{t, y, n, pm, e, phases};
     SampAccS<T> sms{phases, y, n, e};
-    static bool attrs = false;
-    if (!attrs) {
+    static char attrs;
+    if (!setup_done(&attrs)) {
       CUNA_CK(cudaFuncSetAttribute(k_bin_scatter_resv<SampAccS<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)(sizeof(int) * (3 * kScanFuseTiles + 1))));
-      attrs = true;
+      mark_setup_done(&attrs);
     }
     k_bin_count_resv<<<nrb, 512, sizeof(int) * ntiles, st>>>(smp, counts, rsv, ntiles, rspan);
     CUNA_CK(cudaGetLastError());
@@ -334,8 +334,8 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   const int ch2 = 2 * CH;
   // gather: 8 cells per thread on tiles of 2048 cells, else 4
   const bool cw8 = (1 << p->logTL) == 2048;
-  static bool attr_done = false;
-  if (!attr_done) {
+  static char attr_done;
+  if (!setup_done(&attr_done)) {
     const int mx = 200 * 1024;
     CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
@@ -346,7 +346,7 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     CUNA_CK(cudaFuncSetAttribute(k_grid_acc_seg<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_fixed_seg<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_scatter_seg<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    attr_done = true;
+    mark_setup_done(&attr_done);
   }
   size_t smg;
   if (p->grid_method == CUNA2_GRID_GATHER) smg = grid_smem_bytes<T>(p->logTL, p->m);
@@ -401,11 +401,11 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   const int BA = elems / L1, BB = elems / L2, PB = BB / 2;
   const size_t smemA = sizeof(C) * (size_t)BA * fft_pitch(L1, BA);
   const size_t smemB = sizeof(C) * (size_t)BB * fft_pitch(L2, BB);
-  static bool attr2 = false;
-  if (!attr2) {
+  static char attr2;
+  if (!setup_done(&attr2)) {
     CUNA_CK(cudaFuncSetAttribute(k_fft_colpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CUNA_CK(cudaFuncSetAttribute(k_fft_rowpass_acc<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr2 = true;
+    mark_setup_done(&attr2);
   }
   k_fft_colpass<T><<<dim3(L2 / BA, nslab), threads, smemA, st>>>(z, z, f, (int64_t)L);
   CUNA_CK(cudaGetLastError());
@@ -863,10 +863,10 @@ int backward_run(cuna2_plan_st *p, const double *t, const T *y, const typename C
   const double tscale = (double)p->ng / T_;
   const int L = 1 << p->geom.logL;
   if (p->small) {
-    static bool attr = false;
-    if (!attr) {
+    static char attr;
+    if (!setup_done(&attr)) {
       CUNA_CK(cudaFuncSetAttribute(k_bwd_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-      attr = true;
+      mark_setup_done(&attr);
     }
     const size_t smem = sizeof(C) * (size_t)fft_pitch(L, 1);
     const int threads = std::max(32, std::min(sizeof(T) == 4 ? 1024 : 512, L / kFftE));
@@ -893,11 +893,11 @@ int backward_run(cuna2_plan_st *p, const double *t, const T *y, const typename C
   const int BA = elems / L1, BB = elems / L2;
   const size_t smemA = sizeof(C) * (size_t)BA * fft_pitch(L1, BA);
   const size_t smemB = sizeof(C) * (size_t)BB * fft_pitch(L2, BB);
-  static bool attr2 = false;
-  if (!attr2) {
+  static char attr2;
+  if (!setup_done(&attr2)) {
     CUNA_CK(cudaFuncSetAttribute(k_bwd_colpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CUNA_CK(cudaFuncSetAttribute(k_bwd_rowpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr2 = true;
+    mark_setup_done(&attr2);
   }
   k_bwd_colpass<T><<<L2 / BA, threads, smemA, st>>>(sp, z, f);
   CUNA_CK(cudaGetLastError());

@@ -172,12 +172,12 @@ int bct_at(T *grid, const BDesc<T> *D, const int *list, int cnt, typename CxOf<T
   constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
   constexpr int BA = PassCfg<T>::ELEMS >> LOG1;
   constexpr size_t smA = ct_colpass_smem<T, LOGL>(), smB = ct_rowpass_smem<T, LOGL>();
-  static bool attr = false;
-  if (!attr) {
+  static char attr;
+  if (!setup_done(&attr)) {
     if (cudaFuncSetAttribute(k_bct_colpass<T, LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smA) ||
         cudaFuncSetAttribute(k_bct_rowpass<T, LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smB))
       return -1;
-    attr = true;
+    mark_setup_done(&attr);
   }
   k_bct_colpass<T, LOGL><<<dim3((1 << LOG2) / BA, cnt), PassCfg<T>::THREADS, smA, st>>>(grid, D, list);
   if (cudaPeekAtLastError() != cudaSuccess) return -1;
@@ -427,13 +427,13 @@ int batch_run(cuna2_batch_plan_st *p, const double *t, const T *y, typename CxOf
   typedef typename RecOf<T>::type Rec;
   if ((p->n_total > 0 && (!t || !y)) || !F) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL array");
   const BDesc<T> *D = (const BDesc<T> *)p->d_desc;
-  static bool attr = false;
-  if (!attr) {
+  static char attr;
+  if (!setup_done(&attr)) {
     CUNA_CK(cudaFuncSetAttribute(k_bsmall<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     CUNA_CK(cudaFuncSetAttribute(k_bgrid<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CUNA_CK(cudaFuncSetAttribute(k_bcolpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CUNA_CK(cudaFuncSetAttribute(k_browpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr = true;
+    mark_setup_done(&attr);
   }
   // small series on the side stream, overlapping the large-series pipeline
   if (!p->small_classes.empty()) {

@@ -403,12 +403,12 @@ int compat_ct_at(typename CxOf<T>::type *f_hat, typename CxOf<T>::type *scratch,
   constexpr int BA = PassCfg<T>::ELEMS >> LOG1, BB = PassCfg<T>::ELEMS >> LOG2;
   constexpr size_t smA = ct_colpass_smem<T, LOGL>();
   constexpr size_t smB = sizeof(typename CxOf<T>::type) * (size_t)fft_pitch(1 << LOG2, BB) * BB;
-  static bool attr = false;
-  if (!attr) {
+  static char attr;
+  if (!setup_done(&attr)) {
     if (cudaFuncSetAttribute(k_ct_colpass_oop<T, LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smA) ||
         cudaFuncSetAttribute(k_ct_rowpass_compat<T, LOGL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smB))
       return -1;
-    attr = true;
+    mark_setup_done(&attr);
   }
   const int64_t L = (int64_t)1 << LOGL;
   k_ct_colpass_oop<T, LOGL><<<dim3((1 << LOG2) / BA, nbs), PassCfg<T>::THREADS, smA, st>>>(f_hat, scratch, f, L);
@@ -526,11 +526,11 @@ int compat_fft(typename CxOf<T>::type *f_hat, int ng, int nbs, const typename Fp
     const int L = 1 << logL;
     const int threads = max(32, L / kFftE);
     const size_t smem = sizeof(C) * (size_t)fft_pitch(L, 1);
-    static bool attr = false;
-    if (!attr) {
+    static char attr;
+    if (!setup_done(&attr)) {
       CUNA_CK(cudaFuncSetAttribute(k_fft_single_compat<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    200 * 1024));
-      attr = true;
+      mark_setup_done(&attr);
     }
     k_fft_single_compat<T><<<nbs, threads, smem, st>>>(f_hat, f, dfp, norm ? 1 : 0);
     CUNA_CK(cudaGetLastError());
@@ -547,12 +547,12 @@ int compat_fft(typename CxOf<T>::type *f_hat, int ng, int nbs, const typename Fp
   const int BA = elems / L1, BB = elems / L2;
   const size_t smemA = sizeof(C) * (size_t)BA * fft_pitch(L1, BA);
   const size_t smemB = sizeof(C) * (size_t)BB * fft_pitch(L2, BB);
-  static bool attr2 = false;
-  if (!attr2) {
+  static char attr2;
+  if (!setup_done(&attr2)) {
     CUNA_CK(cudaFuncSetAttribute(k_fft_colpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CUNA_CK(cudaFuncSetAttribute(k_fft_rowpass_compat<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  200 * 1024));
-    attr2 = true;
+    mark_setup_done(&attr2);
   }
   const int64_t L = (int64_t)ng;
   k_fft_colpass<T><<<dim3(L2 / BA, nbs), threads, smemA, st>>>(f_hat, scratch, f, L);
@@ -632,14 +632,14 @@ int compat_grid(const T *x, const T *y, typename CxOf<T>::type *f_hat, int n, in
     // count + reserve, then scan + scatter without global atomics (binning.cuh)
     const int64_t span = resv_span(n, ntiles, device_sm_count());
     const size_t sms3 = sizeof(int) * (3 * (size_t)ntiles + 1);
-    static bool attr = false;
-    if (!attr) {
+    static char attr;
+    if (!setup_done(&attr)) {
       const int mx = (int)(sizeof(int) * (3 * kScanFuseTiles + 1));
       CUNA_CK(cudaFuncSetAttribute(k_bin_scatter_resv<SampCompat<T, false>>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
       CUNA_CK(cudaFuncSetAttribute(k_bin_scatter_resv<SampCompat<T, true>>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-      attr = true;
+      mark_setup_done(&attr);
     }
     if (boot) {
       k_bin_count_resv<<<nrb, 512, sizeof(int) * ntiles, st>>>(sb, cw.counts, cw.resv, ntiles, span);

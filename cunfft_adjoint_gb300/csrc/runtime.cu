@@ -4,6 +4,7 @@
 #include <stdio.h>
 #include <map>
 #include <mutex>
+#include <set>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -183,6 +184,25 @@ int *g_timeouts_host = nullptr;
 int *g_timeouts_dev = nullptr;
 std::once_flag g_timeouts_once;
 }  // namespace
+
+namespace {
+std::mutex g_setup_mu;
+std::set<std::pair<int, const void *>> *g_setup = new std::set<std::pair<int, const void *>>();
+}  // namespace
+
+bool setup_done(const void *key) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  std::lock_guard<std::mutex> lk(g_setup_mu);
+  return g_setup->count(std::make_pair(dev, key)) != 0;
+}
+
+void mark_setup_done(const void *key) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> lk(g_setup_mu);
+  g_setup->insert(std::make_pair(dev, key));
+}
 
 int *wait_timeout_counter() {
   std::call_once(g_timeouts_once, [] {

@@ -58,6 +58,13 @@ constexpr int kMaxLogL = 26;
 // hold the whole transform (multi-CTA passes for a single small transform)
 int fft_geometry(bool is_double, int logL, FftGeom *g, bool split = false);
 
+// One-time per-device setup (kernel attributes): setup_done(key) tells whether
+// `key` has been marked on the current device, mark_setup_done(key) marks it.
+// Thread-safe; two threads may both run an idempotent setup before it is
+// marked.
+bool setup_done(const void *key);
+void mark_setup_done(const void *key);
+
 // Device pointer (host-mapped) of the counter of bounded waits that ran out;
 // nullptr when mapped host memory is unavailable (TMA kernels are then not
 // used).
