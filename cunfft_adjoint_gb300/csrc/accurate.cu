@@ -144,7 +144,7 @@ int ct_passes_at(typename CxOf<T>::type *z, const FftDev<T> &f, const AccParams<
   }
   bool tma = false;
   if constexpr (sizeof(T) == 4 && TmaCol<LOGL>::ok) {
-    // column pass through TMA boxes when the driver encodes the tensor map
+    // column pass through TMA boxes when the CUDA driver encodes the tensor map
     int *tmo = tma_enabled() ? wait_timeout_counter() : nullptr;
     alignas(64) CUtensorMap map;
     if (tmo && ct_colpass_tma_map<LOGL>(&map, z, nslab)) {

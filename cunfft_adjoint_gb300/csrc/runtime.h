@@ -77,7 +77,7 @@ int *wait_timeout_counter();
 bool tma_enabled();
 // Tiled 3D tensor map (CUtensorMap, 128 bytes at `map`) over float32 data at
 // `base`: dims {d0, d1, d2} (d0 innermost), byte strides {s1, s2} of
-// dimensions 1 and 2, box {b0, b1, 1}.  Returns false when the driver entry
+// dimensions 1 and 2, box {b0, b1, 1}.  Returns false when the CUDA driver entry
 // point is missing or the encoding is rejected.
 bool encode_tmap_f32_3d(void *map, const void *base, uint64_t d0, uint64_t d1, uint64_t d2, uint64_t s1,
                         uint64_t s2, uint32_t b0, uint32_t b1);

@@ -1,7 +1,7 @@
 /* cuna_oracle.c -- CPU oracle for the adjoint-NFFT path.  TEST INFRASTRUCTURE.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs may
- * load this library, and only as the checker or the timed CPU baseline; the
+ * load this library, and only to verify results or as the timed CPU baseline; the
  * product never routes through it.
  *
  * Contents

@@ -1,7 +1,7 @@
 """numpy/ctypes front end of the CPU oracle.  TEST INFRASTRUCTURE.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs import
-this module, as the checker or as the timed CPU baseline.  The product never
+this module, to verify results or as the timed CPU baseline.  The product never
 imports it.
 
 * ``build()`` compiles oracle/cuna_oracle.c into oracle/liboracle.so (gcc).
