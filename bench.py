@@ -17,8 +17,9 @@ torchrun runs N independent replicas ("replicas only"), value = the sum.
 The reference arm (`--impl reference`) times the reference's pipeline (its
 compat arithmetic: R_f = 6 float filter, non-periodic grid of ng = R*Nf cells,
 unnormalised inverse FFT, deconvolution) as the multi-threaded CPU program of
-the oracle, on the machine's host cores; the reference has no CPU implementation
-of its own and its CUDA sources are not available on the GPU machine.
+the oracle, on the host cores of the machine that runs the benchmark; the
+reference has no CPU implementation of its own, and its CUDA sources are not
+shipped with this package.
 """
 import argparse
 import json

@@ -35,7 +35,7 @@ enum {
   CUNA2_SUCCESS = 0,
   CUNA2_ERROR_INVALID_VALUE = 1, /* bad size, NULL pointer, bad plan       */
   CUNA2_ERROR_CUDA = 2,          /* a CUDA runtime call failed              */
-  CUNA2_ERROR_UNSUPPORTED = 3,   /* size/configuration this build rejects   */
+  CUNA2_ERROR_UNSUPPORTED = 3,   /* size/configuration this library rejects */
   CUNA2_ERROR_ALLOC = 4,         /* device or host allocation failed        */
   CUNA2_ERROR_CUFFT = 5          /* the cuFFT comparator path failed        */
 };

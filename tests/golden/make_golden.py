@@ -11,7 +11,8 @@ oracle.oracle.RefCPU:
     fast_gridding_bootstrap / cunfft_adjoint_raw_async_bootstrap for the
     bootstrap fixtures.
 
-Run in a container that has the reference tree (the GPU machine does not):
+Run where the reference source tree is available (the fixtures it writes
+are committed, so the tests need no reference tree):
     python oracle/build_ref.py && python tests/golden/make_golden.py
 """
 import os
