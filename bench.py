@@ -697,6 +697,13 @@ def main():
                          "traffic": traffic, "algorithmic_bytes": sb.get(dom, 0)},
             "stages_ms": stages,
             "pipeline_gbs": total_bytes / (ms_step * 1e-3) / 1e9,
+            # compulsory traffic only: t and y in, the spectrum out
+            "compulsory_gbs": (n * 12 + nf * 8) / (ms_step * 1e-3) / 1e9,
+            # reported, not a roofline: 2m taps x 3 flops per sample (recurrence
+            # product + fused multiply-add) + 5 L log2 L for the packed L = ng/2
+            # complex FFT
+            "flops_per_transform": 2 * m * 3 * n + 5 * (ng // 2) * int(np.log2(ng // 2)),
+            "tflops": (2 * m * 3 * n + 5 * (ng // 2) * int(np.log2(ng // 2))) / (ms_step * 1e-3) / 1e12,
             "fft_vs_cufft": fft_cmp,
             "e2e": {"value": 1000.0 / e2e_ms, "unit": UNIT, "ms_per_step": e2e_ms, "steps": e2e_steps,
                     "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": nf * 8,
