@@ -139,3 +139,52 @@ def test_no_oracle_in_product():
             if f.endswith((".py", ".cu", ".cuh", ".cpp", ".h")):
                 txt = open(os.path.join(dirpath, f)).read()
                 assert "oracle" not in txt.replace("the oracle", ""), os.path.join(dirpath, f)
+
+
+_C_EXAMPLE = r"""#include <stdio.h>
+#include <stdlib.h>
+#include <cuda_runtime.h>
+#include "cuna2.h"
+
+/* t_d: n doubles, y_d: n floats, F_d: nf float2 values, all in device memory */
+int transform_series(const double *t_d, const float *y_d, float2 *F_d, int64_t n, double t0, double T,
+                     cudaStream_t stream, int count) {
+  cuna2_plan plan;
+  float best_ms = 0.f;
+  if (cuna2_plan_create(&plan, CUNA2_F32, (int64_t)1 << 20, 4, 12) != CUNA2_SUCCESS) {
+    fprintf(stderr, "cuna2: %s\n", cuna2_last_error());
+    return 1;
+  }
+  /* once, on a representative input and before any graph capture */
+  if (cuna2_plan_autotune(plan, t_d, y_d, F_d, n, t0, T, stream, 5, &best_ms) != CUNA2_SUCCESS ||
+      cuna2_plan_set_graph(plan, 1) != CUNA2_SUCCESS) {
+    fprintf(stderr, "cuna2: %s\n", cuna2_last_error());
+    cuna2_plan_destroy(plan);
+    return 1;
+  }
+  for (int i = 0; i < count; ++i)
+    if (cuna2_adjoint(plan, t_d, y_d, F_d, n, t0, T, stream) != CUNA2_SUCCESS) {
+      fprintf(stderr, "cuna2: %s\n", cuna2_last_error());
+      break;
+    }
+  cuna2_plan_destroy(plan);
+  printf("%lld bounded waits ran out\n", cuna2_wait_timeouts());
+  return 0;
+}
+"""
+
+
+def test_c_header_compiles_as_c(tmp_path):
+    """include/cuna2.h is plain C: the accurate-mode example of the
+    integration guide compiles as C11 with every warning an error."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    cuda_inc = "/usr/local/cuda/include"
+    if not gcc or not os.path.exists(os.path.join(cuda_inc, "cuda_runtime.h")):
+        pytest.skip("gcc or the CUDA headers are not installed")
+    src = tmp_path / "example.c"
+    src.write_text(_C_EXAMPLE)
+    out = subprocess.run([gcc, "-std=c11", "-Wall", "-Werror", "-c", str(src), "-I", INC, "-I", cuda_inc,
+                          "-o", str(tmp_path / "example.o")], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
