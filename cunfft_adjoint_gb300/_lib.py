@@ -87,6 +87,13 @@ CORE_SIGNATURES = {
     "cuna2_batch_info": (_I, [_P, _P, _P]),
     "cuna2_batch_set_graph": (_I, [_P, _I]),
     "cuna2_batch_adjoint": (_I, [_P, _P, _P, _P, _P]),
+    "cuna2_inspect_compat_taps_f32": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P]),
+    "cuna2_inspect_compat_taps_f64": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P]),
+    "cuna2_inspect_bootstrap_draws": (_I, [_I, _I, _U, _P, _P]),
+    "cuna2_inspect_compat_bins_f32": (_I, [_P, _P, _I, _I, _P, _I, _P, _P, _I, _P, _P]),
+    "cuna2_inspect_compat_bins_f64": (_I, [_P, _P, _I, _I, _P, _I, _P, _P, _I, _P, _P]),
+    "cuna2_inspect_phases": (_I, [_P, _I64, _D, _D, _I64, _P, _P, _P]),
+    "cuna2_plan_inspect_bins": (_I, [_P, _P, _P, _I64, _D, _D, _P, _P, _I64, _P, _P]),
 }
 
 _core = None

@@ -93,8 +93,10 @@ def build(force=False, verbose=False):
     def compile_dropin(prec):
         out = os.path.join(OBJ, "dropin_%s.o" % prec)
         defs = ["-DDOUBLE_PRECISION"] if prec == "d" else []
-        _run([nvcc()] + NVCC_COMMON + defs + ["-x", "c++", "-c", os.path.join(CSRC, "dropin.cpp"),
-                                              "-o", out], verbose)
+        # host arithmetic of the drop-in (scale_x) rounds like the reference's
+        # on x86 and Arm alike: no fused multiply-add contraction
+        _run([nvcc()] + NVCC_COMMON + defs + ["-Xcompiler", "-ffp-contract=off", "-x", "c++", "-c",
+                                              os.path.join(CSRC, "dropin.cpp"), "-o", out], verbose)
         return out
 
     with ThreadPoolExecutor(max_workers=len(CORE_UNITS) + 2) as ex:

@@ -192,13 +192,22 @@ int ct_passes(int logL, typename CxOf<T>::type *z, const FftDev<T> &f, const Acc
 // With `multi` (nmulti channels of n values, channel-major), the channels are
 // transformed together: one binning pass, one gridding launch with a slab per
 // channel, one slab-batched FFT; outputs F[c*nf + k].
+// Where cuna2_plan_inspect_bins wants the binning's output: the run stops
+// after the binning and copies its tile offsets and records here.
+struct BinOut {
+  int *offsets;
+  void *records;
+  int64_t max_records;
+  int64_t *nrecords;
+};
+
 template <typename T>
 int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>::type *F, int64_t n,
                 double t0, double T_, cudaStream_t st, Prof *pr = nullptr, int nbs = 0, unsigned seed = 0,
-                const T *multi = nullptr, int nmulti = 0) {
+                const T *multi = nullptr, int nmulti = 0, const BinOut *bo = nullptr) {
   typedef typename CxOf<T>::type C;
   typedef typename RecOf<T>::type Rec;
-  if (n < 0 || (n > 0 && (!t || !y)) || !F || !(T_ > 0) || !std::isfinite(T_) || !std::isfinite(t0))
+  if (n < 0 || (n > 0 && (!t || !y)) || (!F && !bo) || !(T_ > 0) || !std::isfinite(T_) || !std::isfinite(t0))
     return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument (n=%lld T=%g)", (long long)n, T_);
   if (n > (int64_t)1 << 30) return fail(CUNA2_ERROR_UNSUPPORTED, "n > 2^30 samples per transform");
   if (nbs < 0 || nbs > 65535 || (int64_t)nbs * n >= ((int64_t)1 << 31))
@@ -256,6 +265,8 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   Rec *recs = (Rec *)(w + o_rec);
   T *grid = (T *)(w + o_grid);
   T *wts = multi ? const_cast<T *>(multi) : (nbs > 0 ? (T *)(w + o_wts) : nullptr);
+  if (bo && (small || seg))
+    return fail(CUNA2_ERROR_UNSUPPORTED, "record inspection needs a tiled plan with the global binning form");
   mark(pr, "start", st);
   if (nbs > 0) {
     static char attrw;
@@ -325,6 +336,19 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     k_scan_tiles<<<1, 1024, 0, st>>>(counts, offsets, cursor, ntiles);
     CUNA_CK(cudaGetLastError());
   }
+  }
+  if (bo) {
+    int total = 0;
+    CUNA_CK(cudaMemcpyAsync(bo->offsets, offsets, sizeof(int) * (ntiles + 1), cudaMemcpyDeviceToDevice, st));
+    CUNA_CK(cudaMemcpyAsync(&total, offsets + ntiles, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUNA_CK(cudaStreamSynchronize(st));
+    if (bo->nrecords) *bo->nrecords = total;
+    if (total > bo->max_records)
+      return fail(CUNA2_ERROR_INVALID_VALUE, "%d records do not fit in max_records = %lld", total,
+                  (long long)bo->max_records);
+    if (total > 0)
+      CUNA_CK(cudaMemcpyAsync(bo->records, recs, sizeof(Rec) * (size_t)total, cudaMemcpyDeviceToDevice, st));
+    return CUNA2_SUCCESS;
   }
   // bootstrap / channels: each CTA grids a group of slabs of one tile, reusing its staged records
   const int group = wts ? std::min(8, nslab) : 1;
@@ -931,4 +955,53 @@ extern "C" int cuna2_adjoint_multi(cuna2_plan p, const double *t, const void *y,
                               nchan);
   return adjoint_run<double>(p, t, (const double *)y, (double2 *)F, n, t0, T, st, nullptr, 0, 0,
                              (const double *)y, nchan);
+}
+
+// ---------------------------------------------------------------------------
+// Integer steps read back (tests and diagnostics; the transforms never call
+// these): the 64-bit fixed-point phase and cell of every sample, from
+// phase_of / cell_of_phase as the binning samplers run them, and the records
+// of a plan's own binning.
+// ---------------------------------------------------------------------------
+namespace cuna {
+namespace {
+__global__ void k_inspect_phases(const double *__restrict__ t, int64_t n, PhaseMul pm, int64_t ng,
+                                 uint64_t *__restrict__ S, int *__restrict__ cell) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t s = phase_of(t[i], pm);
+    int c;
+    float f;
+    cell_of_phase<float>(s, ng, c, f);
+    if (S) S[i] = s;
+    if (cell) cell[i] = c;
+  }
+}
+}  // namespace
+}  // namespace cuna
+
+extern "C" int cuna2_inspect_phases(const double *t, int64_t n, double t0, double T, int64_t ng, uint64_t *phase,
+                                    int *cell, cudaStream_t st) {
+  clear_error();
+  if (n < 0 || (n > 0 && !t) || ng < 1 || ng > ((int64_t)1 << 30) || !(T > 0) || !std::isfinite(T) ||
+      !std::isfinite(t0))
+    return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument (n=%lld ng=%lld T=%g)", (long long)n, (long long)ng, T);
+  if (n == 0) return CUNA2_SUCCESS;
+  const PhaseMul pm = phase_setup(t0, T);
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 8192);
+  k_inspect_phases<<<blocks, 256, 0, st>>>(t, n, pm, ng, phase, cell);
+  CUNA_CK(cudaGetLastError());
+  return CUNA2_SUCCESS;
+}
+
+extern "C" int cuna2_plan_inspect_bins(cuna2_plan p, const double *t, const void *y, int64_t n, double t0, double T,
+                                       int *offsets, void *records, int64_t max_records, int64_t *nrecords,
+                                       cudaStream_t st) {
+  clear_error();
+  if (!p || !offsets || max_records < 0 || (max_records > 0 && !records))
+    return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  const BinOut bo{offsets, records, max_records, nrecords};
+  if (p->dtype == CUNA2_F32)
+    return adjoint_run<float>(p, t, (const float *)y, nullptr, n, t0, T, st, nullptr, 0, 0, nullptr, 0, &bo);
+  return adjoint_run<double>(p, t, (const double *)y, nullptr, n, t0, T, st, nullptr, 0, 0, nullptr, 0, &bo);
 }

@@ -1180,13 +1180,13 @@ __global__ void __launch_bounds__(1024) k_boot_weights(const T *__restrict__ y, 
     for (int p = threadIdx.x; p < n; p += blockDim.x) cnt[p] = 0;
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x)
-      atomicAdd(&cnt[xorshift32(wang_hash(s0 + (unsigned)i)) % (unsigned)n], 1);
+      atomicAdd(&cnt[boot_draw(s0, (unsigned)i, (unsigned)n)], 1);
     __syncthreads();
     for (int p = threadIdx.x; p < n; p += blockDim.x) w[p] = (T)cnt[p] * y[p];
   } else {
     // w was zeroed; adding identical values y[d] is exact in any order
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      const unsigned d = xorshift32(wang_hash(s0 + (unsigned)i)) % (unsigned)n;
+      const unsigned d = boot_draw(s0, (unsigned)i, (unsigned)n);
       atomicAdd(&w[d], y[d]);
     }
   }

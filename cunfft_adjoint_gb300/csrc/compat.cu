@@ -41,10 +41,16 @@ constexpr int kCompatMaxRf = 64;  // shared E3 table size
 // ---------------------------------------------------------------------------
 // filter precompute: set_gpu_filter_properties, src/gaussian_filter.cu:204-228
 // ---------------------------------------------------------------------------
+// Filter origin u = (int)(ng x - R_f) of src/gaussian_filter.cu:213, in the
+// sample's own precision (nvcc contracts the product and the difference into
+// one fused multiply-add, here as in the reference's build).
+__device__ __forceinline__ int compat_origin(float x, int ng, int rf) { return (int)(ng * x - rf); }
+__device__ __forceinline__ int compat_origin(double x, int ng, int rf) { return (int)(ng * x - rf); }
+
 __global__ void k_compat_filter_f32(cuna2_filter_properties_f32 *f, const float *x, int ng, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
-    int u = (int)(ng * x[i] - f->filter_radius);
+    int u = compat_origin(x[i], ng, f->filter_radius);
     float eps = ng * x[i] - u;
     float eps2 = eps / f->b;
     f->E1[i] = expf(-eps * eps2) / sqrtf(CUNA_PI * f->b);
@@ -58,7 +64,7 @@ __global__ void k_compat_filter_f32(cuna2_filter_properties_f32 *f, const float 
 __global__ void k_compat_filter_f64(cuna2_filter_properties_f64 *f, const double *x, int ng, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
-    int u = (int)(ng * x[i] - f->filter_radius);
+    int u = compat_origin(x[i], ng, f->filter_radius);
     double eps = ng * x[i] - u;
     double eps2 = eps / f->b;
     f->E1[i] = exp(-eps * eps2) / sqrt(CUNA_PI * f->b);
@@ -174,7 +180,7 @@ __device__ __forceinline__ void compat_coefs(const typename RecOf<T>::type &rc, 
     int d = rc.p;
     val = (T)1.0;
     if (y) {
-      d = xorshift32(wang_hash(seed + i)) % n;
+      d = (int)boot_draw(seed, (unsigned)i, (unsigned)n);
       val = y[d];
     }
     E1 = E1g[d];
@@ -611,13 +617,12 @@ int check_args(int n, int ng, int nbs, const void *x, const void *f_hat, const v
   return CUNA2_SUCCESS;
 }
 
-// Gridding stage: binning + tiled gridding, accumulating into f_hat.
+// Binning: the bucket sort of the samples into 4096-cell tiles (records
+// in cw.recs, tile t's records at [cw.offsets[t], cw.offsets[t+1])).
 template <typename T>
-int compat_grid(const T *x, const T *y, typename CxOf<T>::type *f_hat, int n, int ng, int nbs,
-                const typename FpOf<T>::type *dfp, unsigned seed, bool boot, const CompatWs &cw,
-                cudaStream_t st) {
+int compat_bin(const T *x, const T *y, int n, int ng, const typename FpOf<T>::type *dfp, bool boot,
+               const CompatWs &cw, cudaStream_t st) {
   typedef typename RecOf<T>::type Rec;
-  if (n == 0) return CUNA2_SUCCESS;
   const int ntiles = (ng + (1 << kCompatLogTL) - 1) >> kCompatLogTL;
   Rec *recs = (Rec *)cw.recs;
   SampCompat<T, false> sp{x, y, dfp, n, ng};
@@ -661,6 +666,19 @@ int compat_grid(const T *x, const T *y, typename CxOf<T>::type *f_hat, int n, in
     else k_bin_scatter<<<gscat, 512, 2 * smc, st>>>(sp, cw.offsets, cw.cursor, recs, ntiles);
     CUNA_CK(cudaGetLastError());
   }
+  return CUNA2_SUCCESS;
+}
+
+// Gridding stage: binning + tiled gridding, accumulating into f_hat.
+template <typename T>
+int compat_grid(const T *x, const T *y, typename CxOf<T>::type *f_hat, int n, int ng, int nbs,
+                const typename FpOf<T>::type *dfp, unsigned seed, bool boot, const CompatWs &cw,
+                cudaStream_t st) {
+  typedef typename RecOf<T>::type Rec;
+  if (n == 0) return CUNA2_SUCCESS;
+  const int ntiles = (ng + (1 << kCompatLogTL) - 1) >> kCompatLogTL;
+  CUNA_TRY(compat_bin<T>(x, y, n, ng, dfp, boot, cw, st));
+  Rec *recs = (Rec *)cw.recs;
   const size_t smg = compat_grid_smem<T>();
   if (boot)
     k_grid_compat<T, true><<<dim3(ntiles, nbs), 256, smg, st>>>(recs, cw.offsets, f_hat, ng, dfp, y, n, seed);
@@ -784,6 +802,110 @@ extern "C" int cuna2_compat_normalize_f64(double2 *f_hat, int ng, int nbatch,
 }
 
 // ---------------------------------------------------------------------------
+// Integer steps read back: per sample the cell j, the filter origin u and the
+// tap range, the bootstrap draws, and the records of the binning, computed by
+// the same device functions the transforms run (compat_taps, compat_origin,
+// boot_draw, compat_bin).  Tests compare them with the oracle bit for bit;
+// the transforms never call these.
+// ---------------------------------------------------------------------------
+namespace cuna {
+namespace {
+
+template <typename T>
+__global__ void k_inspect_compat_taps(const T *x, int n, int ng, int rf, int clamp, int *cell, int *origin,
+                                      int *tlo, int *thi) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T xi = x[i];
+  int j = 0, ms = 0, me = 0;
+  const bool any = compat_taps((double)xi, ng, rf, clamp != 0, j, ms, me);
+  if (cell) cell[i] = j;
+  if (origin) origin[i] = compat_origin(xi, ng, rf);
+  if (tlo) tlo[i] = any ? ms : 0;
+  if (thi) thi[i] = any ? me : 0;
+}
+
+__global__ void k_inspect_draws(unsigned n, int64_t total, unsigned seed, int *d) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+    d[i] = (int)boot_draw(seed, (unsigned)i, n);
+}
+
+template <typename T>
+int inspect_compat_taps(const T *x, int n, int ng, int clamp, int *cell, int *origin, int *tlo, int *thi,
+                        cudaStream_t st) {
+  clear_error();
+  if (n < 0 || ng < 1 || (n > 0 && !x))
+    return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument (n=%d ng=%d)", n, ng);
+  if (n == 0) return CUNA2_SUCCESS;
+  const int rf = sizeof(T) == 4 ? 6 : 12;
+  k_inspect_compat_taps<T><<<(n + 255) / 256, 256, 0, st>>>(x, n, ng, rf, clamp, cell, origin, tlo, thi);
+  CUNA_CK(cudaGetLastError());
+  return CUNA2_SUCCESS;
+}
+
+template <typename T>
+int inspect_compat_bins(const T *x, const T *y, int n, int ng, const typename FpOf<T>::type *dfp, int boot,
+                        int *offsets, void *records, int max_records, int *nrecords, cudaStream_t st) {
+  typedef typename RecOf<T>::type Rec;
+  clear_error();
+  CUNA_TRY(check_args(n, ng, 1, x, offsets, dfp));
+  if (max_records < 0 || (max_records > 0 && !records))
+    return fail(CUNA2_ERROR_INVALID_VALUE, "invalid record buffer (max_records=%d)", max_records);
+  const int ntiles = (ng + (1 << kCompatLogTL) - 1) >> kCompatLogTL;
+  int total = 0;
+  if (n == 0) {
+    CUNA_CK(cudaMemsetAsync(offsets, 0, sizeof(int) * (ntiles + 1), st));
+  } else {
+    CompatWs cw;
+    CUNA_TRY(compat_workspace<T>(n, ng, 1, false, st, &cw));
+    CUNA_TRY(compat_bin<T>(x, y, n, ng, dfp, boot != 0, cw, st));
+    CUNA_CK(cudaMemcpyAsync(offsets, cw.offsets, sizeof(int) * (ntiles + 1), cudaMemcpyDeviceToDevice, st));
+    CUNA_CK(cudaMemcpyAsync(&total, cw.offsets + ntiles, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUNA_CK(cudaStreamSynchronize(st));
+    if (total > max_records) {
+      if (nrecords) *nrecords = total;
+      return fail(CUNA2_ERROR_INVALID_VALUE, "%d records do not fit in max_records = %d", total, max_records);
+    }
+    if (total > 0)
+      CUNA_CK(cudaMemcpyAsync(records, cw.recs, sizeof(Rec) * (size_t)total, cudaMemcpyDeviceToDevice, st));
+  }
+  if (nrecords) *nrecords = total;
+  return CUNA2_SUCCESS;
+}
+
+}  // namespace
+}  // namespace cuna
+
+extern "C" int cuna2_inspect_compat_taps_f32(const float *x, int n, int ng, int clamp, int *cell, int *origin,
+                                             int *tap_lo, int *tap_hi, cudaStream_t st) {
+  return inspect_compat_taps<float>(x, n, ng, clamp, cell, origin, tap_lo, tap_hi, st);
+}
+extern "C" int cuna2_inspect_compat_taps_f64(const double *x, int n, int ng, int clamp, int *cell, int *origin,
+                                             int *tap_lo, int *tap_hi, cudaStream_t st) {
+  return inspect_compat_taps<double>(x, n, ng, clamp, cell, origin, tap_lo, tap_hi, st);
+}
+extern "C" int cuna2_inspect_bootstrap_draws(int n, int nbs, unsigned int seed, int *draw, cudaStream_t st) {
+  clear_error();
+  if (n < 1 || nbs < 1 || !draw || (int64_t)n * nbs > INT_MAX)
+    return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument (n=%d nbs=%d)", n, nbs);
+  const int64_t total = (int64_t)n * nbs;
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, 8192);
+  k_inspect_draws<<<blocks, 256, 0, st>>>((unsigned)n, total, seed, draw);
+  CUNA_CK(cudaGetLastError());
+  return CUNA2_SUCCESS;
+}
+extern "C" int cuna2_inspect_compat_bins_f32(const float *x, const float *y, int n, int ng,
+                                             const cuna2_filter_properties_f32 *d, int boot, int *offsets,
+                                             void *records, int max_records, int *nrecords, cudaStream_t st) {
+  return inspect_compat_bins<float>(x, y, n, ng, d, boot, offsets, records, max_records, nrecords, st);
+}
+extern "C" int cuna2_inspect_compat_bins_f64(const double *x, const double *y, int n, int ng,
+                                             const cuna2_filter_properties_f64 *d, int boot, int *offsets,
+                                             void *records, int max_records, int *nrecords, cudaStream_t st) {
+  return inspect_compat_bins<double>(x, y, n, ng, d, boot, offsets, records, max_records, nrecords, st);
+}
+
+// ---------------------------------------------------------------------------
 // cuna2_compat_adjoint_noalloc_f32: cuna2_compat_adjoint_f32 for callers that
 // cannot allocate device memory.
 //
@@ -859,6 +981,14 @@ int noalloc_setup(int dev, cudaStream_t st, NoAllocDev **out) {
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   NoAllocDev &d = g_noalloc[dev];
   if (!d.ready) {
+    // set-up launches kernels and synchronises the stream, which a stream
+    // capture cannot contain: refuse before touching anything
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CUNA_CK(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone)
+      return fail(CUNA2_ERROR_UNSUPPORTED,
+                  "no-allocation entry point: the first call on a device sets it up and must come before any "
+                  "stream capture");
     void *p = nullptr;
     CUNA_CK(cudaGetSymbolAddress(&p, cuna_noalloc_scratch));
     d.base = (unsigned char *)p;
@@ -882,9 +1012,9 @@ int noalloc_setup(int dev, cudaStream_t st, NoAllocDev **out) {
       if (logL > kSingleLogF32) {
         CUNA_TRY(noalloc_table(tw, used, nlo, 1, L, &f.twlo, st));
         CUNA_TRY(noalloc_table(tw, used, L / nlo, nlo, L, &f.twhi, st));
-      } else {
-        f.twlo = f.tw1;
-        f.twhi = f.tw1;
+      } else {  // single-CTA lengths read tw1 only
+        f.twlo = nullptr;
+        f.twhi = nullptr;
       }
     }
     CUNA_CK(cudaFuncSetAttribute(k_fft_single_compat<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -237,12 +237,21 @@ unsigned int nextPowerOfTwo(unsigned int v) {
 
 dTyp seconds(clock_t dt) { return ((dTyp)dt) / ((dTyp)CLOCKS_PER_SEC); }
 
+// scale_x, src/utils.cu:84-93, with the reference's exact arithmetic: the
+// loop subtracts the CURRENT x[0], which its first pass has already turned
+// into -1/2, so x[0] becomes -1/2 and every later element becomes
+// (x[i] + 1/2) / (x[size-1] - x[0]) - 1/2 with the range taken before the
+// loop.  Callers who wanted [-1/2, 1/2] get it only when x[0] == -1/2 on
+// entry; accurate mode (cuna2_plan_*) takes t0 and T instead and needs no
+// rescaling.  The expressions keep the reference's types (a double
+// reciprocal stored in dTyp, the 0.5 subtracted in double) and this file is
+// compiled without floating-point contraction, so the bits match the
+// reference's on every host.  size < 1 returns (the reference reads x[-1]).
 void scale_x(dTyp *x, int size) {
   if (size < 1) return;
-  const dTyp x0 = x[0];
-  const dTyp invrange = 1. / (x[size - 1] - x0);
+  dTyp invrange = 1. / (x[size - 1] - x[0]);
   for (int i = 0; i < size; i++) {
-    x[i] -= x0;
+    x[i] -= x[0];
     x[i] *= invrange;
     x[i] -= 0.5;
   }

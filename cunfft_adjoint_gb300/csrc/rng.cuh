@@ -22,6 +22,11 @@ __device__ __forceinline__ unsigned xorshift32(unsigned s) {
   s ^= (s << 5);
   return s;
 }
+// draw number i of the stream: the sample index d = xorshift32(wang_hash(
+// seed + i)) % n (src/gridding.cu:101, unsigned arithmetic throughout)
+__device__ __forceinline__ unsigned boot_draw(unsigned seed, unsigned i, unsigned n) {
+  return xorshift32(wang_hash(seed + i)) % n;
+}
 
 }  // namespace
 }  // namespace cuna

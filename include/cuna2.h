@@ -325,6 +325,74 @@ int cuna2_batch_set_graph(cuna2_batch_plan plan, int enable);
 int cuna2_batch_adjoint(cuna2_batch_plan plan, const double *t, const void *y, void *F,
                         cudaStream_t stream);
 
+/* ---------------------------------------------------------------------- */
+/* integer steps read back (tests and diagnostics, not a transform path)   */
+/* ---------------------------------------------------------------------- */
+/* Each of these runs the same device functions as the transforms and writes
+ * what they computed, so that callers can compare the integer steps with a
+ * CPU restatement bit for bit.  Output arrays are device memory; any per-
+ * sample output may be NULL. */
+
+/* Compat mode, per sample i < n (x as for cuna2_compat_adjoint_*):
+ *   cell[i]    j = (int)((x_i + 1/2)(ng - 1)), evaluated in double, clamped
+ *              to [0, ng) when clamp != 0 (fast_gridding, src/gridding.cu:
+ *              43-45) and left unclamped otherwise (fast_gridding_bootstrap,
+ *              src/gridding.cu:93-95);
+ *   origin[i]  u = (int)(ng x_i - R_f) of the filter coefficients
+ *              (set_gpu_filter_properties, src/gaussian_filter.cu:213);
+ *   tap_lo[i], tap_hi[i]  the taps m in [tap_lo, tap_hi) that reach the
+ *              grid (src/gridding.cu:53-58); (0, 0) when none does, which
+ *              includes |j| > 2^30, where the reference's int arithmetic
+ *              overflows. */
+int cuna2_inspect_compat_taps_f32(const float *x, int n, int ng, int clamp, int *cell, int *origin,
+                                  int *tap_lo, int *tap_hi, cudaStream_t stream);
+int cuna2_inspect_compat_taps_f64(const double *x, int n, int ng, int clamp, int *cell, int *origin,
+                                  int *tap_lo, int *tap_hi, cudaStream_t stream);
+
+/* The bootstrap draw stream of both modes: draw[b*n + i] = xorshift32(
+ * wang_hash(seed + b*n + i)) % n for resample b < nbs and draw i < n
+ * (src/gridding.cu:67-82,101).  n*nbs <= INT_MAX. */
+int cuna2_inspect_bootstrap_draws(int n, int nbs, unsigned int seed, int *draw, cudaStream_t stream);
+
+/* The bucket sort in front of compat gridding, as cuna2_compat_adjoint_*
+ * (boot == 0) or cuna2_compat_bootstrap_* (boot != 0) runs it: each sample
+ * is binned into every 4096-cell tile its taps reach.  offsets (ngt + 1 ints,
+ * ngt = ceil(ng / 4096)) delimit tile t's records [offsets[t], offsets[t+1]);
+ * records receives them (at most max_records) and *nrecords their number
+ * (a host int).  Record layout, float (16 bytes): {int cell; float E1;
+ * float E2; int value_bits} (boot == 0) or {int cell; int -, -; int sample}
+ * (boot != 0); double (32 bytes): {int cell; int sample; double E1, E2,
+ * value}, the sample index set only when boot != 0.  Within a tile the
+ * records form a set: their order depends on scheduling and on nothing the
+ * results depend on.  Synchronises `stream`. */
+int cuna2_inspect_compat_bins_f32(const float *x, const float *y, int n, int ng,
+                                  const cuna2_filter_properties_f32 *d_fprops, int boot, int *offsets,
+                                  void *records, int max_records, int *nrecords, cudaStream_t stream);
+int cuna2_inspect_compat_bins_f64(const double *x, const double *y, int n, int ng,
+                                  const cuna2_filter_properties_f64 *d_fprops, int boot, int *offsets,
+                                  void *records, int max_records, int *nrecords, cudaStream_t stream);
+
+/* Accurate mode's grid-index reduction per sample: phase[i] = frac((t_i -
+ * t0)/T) 2^64 as an unsigned 64-bit fixed-point number ((t_i A - t0 A) mod
+ * 2^64, A = 2^64/T to 64 significant bits, each product truncated) and
+ * cell[i] = floor(phase[i] ng / 2^64), for a grid of ng <= 2^30 cells. */
+int cuna2_inspect_phases(const double *t, int64_t n, double t0, double T, int64_t ng, uint64_t *phase,
+                         int *cell, cudaStream_t stream);
+
+/* The plan's own binning of (t, y) as cuna2_adjoint runs it (tiled plans
+ * with the global binning form; other plans return CUNA2_ERROR_UNSUPPORTED):
+ * offsets (ntiles + 1 ints, ntiles = ng / 2^log_tile of the plan's
+ * schedule), the records (at most max_records) and *nrecords (host).  Each
+ * sample gives a record in every tile that its taps cell-m+1 .. cell+m (mod
+ * ng) reach.  Record layout, float plans (16 bytes): {int cell; float frac;
+ * float y; int sample}, frac the fractional cell (the top 24 bits of the low
+ * word of phase*ng, scaled by 2^-24); double plans (32 bytes): {int cell; int
+ * sample; double frac (top 53 bits, scaled by 2^-53); double y; double 0}.
+ * Within a tile the records form a set.  Synchronises `stream`. */
+int cuna2_plan_inspect_bins(cuna2_plan plan, const double *t, const void *y, int64_t n, double t0, double T,
+                            int *offsets, void *records, int64_t max_records, int64_t *nrecords,
+                            cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

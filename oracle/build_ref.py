@@ -1,12 +1,15 @@
 """Recipe: build the reference library's own sources for the CPU (oracle only).
 
 Test infrastructure.  Reads src/gridding.cu, src/gaussian_filter.cu,
-src/cuna_kernel.cu and src/cufft_utils.cu where they lie in the reference tree
-(default /root/reference, override with CUNA_REFERENCE_DIR), rewrites each
-``kern<<<grid, block, ...>>>(args)`` launch into ``CUNA_CPU_LAUNCH(grid, block,
-kern, args)`` on the fly, and pipes the result straight into g++ together with
-the host stand-ins in oracle/refcpu/.  No reference source is copied anywhere;
-the only outputs are object files and two shared libraries in oracle/_ref/:
+src/cuna_kernel.cu, src/cufft_utils.cu, src/utils.cu and src/cuna.cpp where
+they lie in the reference tree (the directory named by CUNA_REFERENCE_DIR),
+rewrites each ``kern<<<grid, block, ...>>>(args)`` launch into
+``CUNA_CPU_LAUNCH(grid, block, kern, args)`` on the fly (and drops
+src/utils.cu's DOUBLE_PRECISION block, a compare-and-swap atomicAdd for GPUs
+without a native double atomic, which the host stand-in replaces), and pipes
+the result straight into g++ together with the host stand-ins in
+oracle/refcpu/.  No reference source is copied anywhere; the only outputs are
+object files and two shared libraries in oracle/_ref/:
 
     oracle/_ref/libcuna_refcpu_f.so   (float build, like libcunaf.so)
     oracle/_ref/libcuna_refcpu_d.so   (-DDOUBLE_PRECISION, like libcunad.so)
@@ -29,9 +32,10 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 SHIM = os.path.join(HERE, "refcpu")
-REF_SOURCES = ["gridding.cu", "gaussian_filter.cu", "cuna_kernel.cu", "cufft_utils.cu"]
+REF_SOURCES = ["gridding.cu", "gaussian_filter.cu", "cuna_kernel.cu", "cufft_utils.cu", "utils.cu", "cuna.cpp"]
 
 _LAUNCH = re.compile(r"(\w+)\s*<<<(.*?)>>>\s*\(", re.S)
+_DOUBLE_ATOMIC = re.compile(r"^#ifdef DOUBLE_PRECISION\s*\n.*?^#endif[^\n]*\n", re.S | re.M)
 
 
 def _rewrite_launches(src: str) -> str:
@@ -42,8 +46,22 @@ def _rewrite_launches(src: str) -> str:
     return _LAUNCH.sub(repl, src)
 
 
+def _drop_double_atomic(src: str) -> str:
+    """src/utils.cu:28-44 defines atomicAdd(double *, double) by a CAS loop;
+    the host stand-in provides that overload instead."""
+    out, n = _DOUBLE_ATOMIC.subn("", src, count=1)
+    if n != 1 or "atomicCAS" in out:
+        raise RuntimeError("build_ref: the DOUBLE_PRECISION atomicAdd block of utils.cu was not found")
+    return out
+
+
 def reference_dir():
-    return os.environ.get("CUNA_REFERENCE_DIR", "/root/reference")
+    """The reference tree: CUNA_REFERENCE_DIR when set, else a directory
+    named ``reference`` beside this repository."""
+    env = os.environ.get("CUNA_REFERENCE_DIR")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 def libs_present():
@@ -58,7 +76,7 @@ def build(verbose=False):
         return False
     os.makedirs(OUT, exist_ok=True)
     inc = os.path.join(ref, "inc")
-    base = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-w",
+    base = ["g++", "-std=c++17", "-fext-numeric-literals", "-O2", "-fPIC", "-ffp-contract=off", "-w",
             "-DBLOCK_SIZE=256", "-I", SHIM, "-I", inc,
             "-include", os.path.join(SHIM, "cuda_runtime.h")]
 
@@ -72,6 +90,8 @@ def build(verbose=False):
         else:
             with open(os.path.join(ref, "src", name)) as f:
                 src = _rewrite_launches(f.read())
+            if name == "utils.cu":
+                src = _drop_double_atomic(src)
             cmd = base + defs + ["-x", "c++", "-c", "-", "-o", obj]
             subprocess.run(cmd, input=src.encode(), check=True)
         return obj

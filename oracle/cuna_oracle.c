@@ -22,6 +22,11 @@
  *   5. cpu_pipeline_* the reference pipeline (compat math) as a multi-threaded
  *                 CPU program: per-thread private grids + reduction, radix-2
  *                 FFT, deconvolution.  This is the timed CPU baseline.
+ *   6. ndft_grad  FP64 direct-sum gradient through the adjoint NDFT.
+ *   7. integer steps per sample: the compat cell, filter origin and tap
+ *                 range, the bootstrap draws, and accurate mode's 64-bit
+ *                 fixed-point phase, cell and fractional cell -- the values
+ *                 the GPU must reproduce bit for bit.
  *
  * Build: gcc -O2 -fopenmp -fPIC -shared -ffp-contract=off (oracle/oracle.py).
  * -ffp-contract=off keeps float rounding identical on x86 and Arm; where the
@@ -506,5 +511,148 @@ void cuna_oracle_ndft_grad(const double *t, const double *y, int64_t n, double t
     }
     gy[j] = sy;
     gt[j] = y[j] * 2.0 * M_PI / T * st;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* 7. integer steps, per sample (checkers of the device's integer outputs)   */
+/* ------------------------------------------------------------------------ */
+
+/* Tap range [ms, me) of cell j, src/gridding.cu:53-58 / :105-110.  The
+ * reference forms j + mend in int arithmetic, which overflows (and then
+ * writes out of bounds) for |j| near 2^31; the drop-in library treats any
+ * |j| > 2^30 as a sample without taps, and so does this restatement.  An
+ * empty range is reported as (0, 0). */
+static void compat_tap_range(int j, int ng, int rf, int *ms_out, int *me_out) {
+  int ms = -rf + 1, me = rf;
+  if (j > (1 << 30) || j < -(1 << 30)) {
+    *ms_out = 0;
+    *me_out = 0;
+    return;
+  }
+  if (j + ms < 0) ms = -j;
+  if (j + me > ng) me = ng - j;
+  if (ms >= me) ms = me = 0;
+  *ms_out = ms;
+  *me_out = me;
+}
+
+/* Per sample i: cell j (src/gridding.cu:43-45, clamped when `clamp`, as
+ * fast_gridding; unclamped as fast_gridding_bootstrap, :93-95), filter
+ * origin u = (int)(ng*x - R_f) (src/gaussian_filter.cu:213; nvcc contracts
+ * the product and difference into one fused multiply-add, so the restatement
+ * rounds once) and the tap range [ms, me).  Any output may be NULL. */
+void cuna_oracle_compat_taps_f32(const float *x, int n, int ng, int clamp, int *j_out, int *u_out,
+                                 int *ms_out, int *me_out) {
+  const int rf = RF_F32;
+  for (int i = 0; i < n; ++i) {
+    const int j = cuna_oracle_compat_cell((double)x[i], ng, clamp);
+    int ms, me;
+    compat_tap_range(j, ng, rf, &ms, &me);
+    if (j_out) j_out[i] = j;
+    if (u_out) u_out[i] = trunc_sat_int((double)fmaf((float)ng, x[i], -(float)rf));
+    if (ms_out) ms_out[i] = ms;
+    if (me_out) me_out[i] = me;
+  }
+}
+
+void cuna_oracle_compat_taps_f64(const double *x, int n, int ng, int clamp, int *j_out, int *u_out,
+                                 int *ms_out, int *me_out) {
+  const int rf = RF_F64;
+  for (int i = 0; i < n; ++i) {
+    const int j = cuna_oracle_compat_cell(x[i], ng, clamp);
+    int ms, me;
+    compat_tap_range(j, ng, rf, &ms, &me);
+    if (j_out) j_out[i] = j;
+    if (u_out) u_out[i] = trunc_sat_int(fma((double)ng, x[i], -(double)rf));
+    if (ms_out) ms_out[i] = ms;
+    if (me_out) me_out[i] = me;
+  }
+}
+
+/* All draws of nbs resamples: d[i] for i < n*nbs, src/gridding.cu:101. */
+void cuna_oracle_bootstrap_draws(uint32_t seed, int n, int nbs, int *d) {
+  const int64_t total = (int64_t)n * nbs;
+  for (int64_t i = 0; i < total; ++i)
+    d[i] = (int)(cuna_oracle_xorshift(cuna_oracle_wang_hash(seed + (uint32_t)i)) % (uint32_t)n);
+}
+
+/* Accurate mode's grid-index reduction (no reference counterpart: the
+ * reference takes x already scaled to [-1/2, 1/2]).  The phase of time t is
+ * the unsigned 64-bit fixed-point number S = frac((t - t0)/T) 2^64, formed as
+ * (t A - t0 A) mod 2^64 with A = 2^64/T held as a 64-bit significand mA and
+ * a binary exponent eA, each product t*A truncated toward zero in magnitude
+ * and negated in two's complement for negative t.  Then cell =
+ * floor(S ng / 2^64) and the fractional cell is the low 64 bits of S ng.
+ * Written from that definition with 128-bit integers. */
+static uint64_t phase_times_ref(double t, uint64_t mA, int eA) {
+  uint64_t u;
+  memcpy(&u, &t, 8);
+  const int ex = (int)((u >> 52) & 0x7FF);
+  if (ex == 0x7FF) return 0;
+  uint64_t mt = u & 0x000FFFFFFFFFFFFFull;
+  int et;
+  if (ex == 0) {
+    et = -1074;
+  } else {
+    mt |= 0x0010000000000000ull;
+    et = ex - 1075;
+  }
+  /* |t| A = mt mA 2^(et + eA), a product of up to 117 bits */
+  const unsigned __int128 prod = (unsigned __int128)mt * mA;
+  const int sh = et + eA;
+  uint64_t r;
+  if (sh >= 64) r = 0;                                  /* a multiple of 2^64 */
+  else if (sh >= 0) r = (uint64_t)(prod << sh);         /* mod 2^64 */
+  else if (sh > -128) r = (uint64_t)(prod >> (-sh));    /* truncation */
+  else r = 0;
+  return (u >> 63) ? (uint64_t)(0 - r) : r;
+}
+
+void cuna_oracle_phase_setup(double t0, double T, uint64_t *mA_out, int *eA_out, uint64_t *B_out) {
+  uint64_t u;
+  memcpy(&u, &T, 8);
+  const int ex = (int)((u >> 52) & 0x7FF);
+  uint64_t mT = u & 0x000FFFFFFFFFFFFFull;
+  int eT;
+  if (ex == 0) {
+    eT = -1074;
+    while (!(mT & 0x0010000000000000ull)) {
+      mT <<= 1;
+      --eT;
+    }
+  } else {
+    mT |= 0x0010000000000000ull;
+    eT = ex - 1075;
+  }
+  /* 2^64 / T = floor(2^116 / mT) 2^(64 - 116 - eT), the significand kept
+   * below 2^64 */
+  unsigned __int128 q = ((unsigned __int128)1 << 116) / mT;
+  int eA = 64 - 116 - eT;
+  if (q >> 64) {
+    q >>= 1;
+    eA += 1;
+  }
+  *mA_out = (uint64_t)q;
+  *eA_out = eA;
+  *B_out = phase_times_ref(t0, (uint64_t)q, eA);
+}
+
+/* Per sample: S, the cell, and the fractional cell as the float path stores
+ * it (the top 24 bits of the low word, an exact 24-bit integer) and as the
+ * double path stores it (the top 53 bits).  Any output may be NULL. */
+void cuna_oracle_phases(const double *t, int64_t n, double t0, double T, int64_t ng, uint64_t *S_out,
+                        int *cell_out, uint32_t *frac24_out, uint64_t *frac53_out) {
+  uint64_t mA, B;
+  int eA;
+  cuna_oracle_phase_setup(t0, T, &mA, &eA, &B);
+  for (int64_t i = 0; i < n; ++i) {
+    const uint64_t S = phase_times_ref(t[i], mA, eA) - B;
+    const unsigned __int128 p = (unsigned __int128)S * (uint64_t)ng;
+    const uint64_t lo = (uint64_t)p;
+    if (S_out) S_out[i] = S;
+    if (cell_out) cell_out[i] = (int)(p >> 64);
+    if (frac24_out) frac24_out[i] = (uint32_t)(lo >> 40);
+    if (frac53_out) frac53_out[i] = lo >> 11;
   }
 }

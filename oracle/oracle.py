@@ -263,6 +263,13 @@ class RefCPU:
         L.refcpu_adjoint_raw.argtypes = [_P, _P, _P, _I, _I]
         L.refcpu_adjoint_raw_async.argtypes = [_P, _P, _P, _I, _I]
         L.refcpu_adjoint_bootstrap.argtypes = [_P, _P, _P, _I, _I, _I, _U]
+        L.refcpu_plan_adjoint.argtypes = [_P, _P, _I, _I, _U, _P, _P]
+        tag_f = "f" if self.dt == np.float32 else "d"
+        self._scale_x = getattr(L, "_Z7scale_xP%si" % tag_f)
+        self._scale_x.argtypes = [_P, _I]
+        self._next_pow2 = L._Z14nextPowerOfTwoj
+        self._next_pow2.argtypes = [_U]
+        self._next_pow2.restype = _U
 
     @staticmethod
     def available(prec="f"):
@@ -299,8 +306,105 @@ class RefCPU:
         fn(_p(x), _p(y), _p(f), len(x), ng)
         return f
 
+    def scale_x(self, x):
+        """scale_x (src/utils.cu:84-93) applied in place to a copy of x."""
+        x = np.array(x, self.dt)
+        self._scale_x(_p(x), len(x))
+        return x
+
+    def next_power_of_two(self, v):
+        """nextPowerOfTwo (src/utils.cu:55-65)."""
+        return int(self._next_pow2(v & 0xFFFFFFFF))
+
+    def plan_adjoint(self, x, y, ng, flags):
+        """init_plan + cunfft_adjoint_from_plan + copyResultsToCPU: (f_hat,
+        f_hat_win or None)."""
+        x = self._in(x); y = self._in(y)
+        f = np.zeros(ng, self.ct)
+        w = np.zeros(ng, self.ct)
+        self.L.refcpu_plan_adjoint(_p(x), _p(y), len(x), ng, flags, _p(f), _p(w))
+        return f, (w if flags & 0x04 else None)
+
     def adjoint_bootstrap(self, x, y, ng, nbs, seed):
         x = self._in(x); y = self._in(y)
         f = np.zeros(nbs * ng, self.ct)
         self.L.refcpu_adjoint_bootstrap(_p(x), _p(y), _p(f), len(x), ng, nbs, seed & 0xFFFFFFFF)
         return f.reshape(nbs, ng)
+
+
+# --------------------------------------------------------------------------
+# integer steps per sample (bit-exact checkers)
+# --------------------------------------------------------------------------
+
+def _declare_int(L):
+    if getattr(L, "_int_declared", False):
+        return
+    L.cuna_oracle_compat_taps_f32.argtypes = [_P, _I, _I, _I, _P, _P, _P, _P]
+    L.cuna_oracle_compat_taps_f64.argtypes = [_P, _I, _I, _I, _P, _P, _P, _P]
+    L.cuna_oracle_bootstrap_draws.argtypes = [_U, _I, _I, _P]
+    L.cuna_oracle_phase_setup.argtypes = [_D, _D, _P, _P, _P]
+    L.cuna_oracle_phases.argtypes = [_P, _I64, _D, _D, _I64, _P, _P, _P, _P]
+    L._int_declared = True
+
+
+def compat_taps(x, ng, prec, clamp=True):
+    """(j, u, ms, me) per sample: the cell of src/gridding.cu:43-45 (clamped
+    when `clamp`), the filter origin of src/gaussian_filter.cu:213 and the tap
+    range of src/gridding.cu:53-58 ((0, 0) when empty)."""
+    L = lib(); _declare_int(L)
+    dt = _dt(prec)
+    x = np.ascontiguousarray(x, dtype=dt)
+    n = len(x)
+    out = [np.empty(n, np.int32) for _ in range(4)]
+    fn = L.cuna_oracle_compat_taps_f32 if dt == np.float32 else L.cuna_oracle_compat_taps_f64
+    fn(_p(x), n, ng, 1 if clamp else 0, *[_p(o) for o in out])
+    return tuple(out)
+
+
+def compat_tiles(j, ms, me, log_tile=12):
+    """Tiles a compat sample's taps touch: (first, last) tile of [j+ms, j+me-1]
+    with 2^log_tile-cell tiles; rows with an empty range give (-1, -1)."""
+    j = np.asarray(j, np.int64); ms = np.asarray(ms, np.int64); me = np.asarray(me, np.int64)
+    has = ms < me
+    t0 = np.where(has, (j + ms) >> log_tile, -1)
+    t1 = np.where(has, (j + me - 1) >> log_tile, -1)
+    return t0, t1
+
+
+def bootstrap_draws_all(seed, n, nbs):
+    """d[b, i] for resample b < nbs and draw i < n (src/gridding.cu:101)."""
+    L = lib(); _declare_int(L)
+    d = np.empty(n * nbs, np.int32)
+    L.cuna_oracle_bootstrap_draws(seed & 0xFFFFFFFF, n, nbs, _p(d))
+    return d.reshape(nbs, n)
+
+
+def phase_setup(t0, T):
+    L = lib(); _declare_int(L)
+    mA = np.zeros(1, np.uint64); eA = np.zeros(1, np.int32); B = np.zeros(1, np.uint64)
+    L.cuna_oracle_phase_setup(float(t0), float(T), _p(mA), _p(eA), _p(B))
+    return int(mA[0]), int(eA[0]), int(B[0])
+
+
+def phases(t, t0, T, ng):
+    """Accurate mode's grid-index reduction per sample: (S, cell, frac24,
+    frac53) with S = frac((t - t0)/T) 2^64 in 64-bit fixed point, cell =
+    floor(S ng / 2^64), and the fractional cell's top 24 / 53 bits."""
+    L = lib(); _declare_int(L)
+    t = np.ascontiguousarray(t, np.float64)
+    n = len(t)
+    S = np.empty(n, np.uint64); cell = np.empty(n, np.int32)
+    f24 = np.empty(n, np.uint32); f53 = np.empty(n, np.uint64)
+    L.cuna_oracle_phases(_p(t), n, float(t0), float(T), int(ng), _p(S), _p(cell), _p(f24), _p(f53))
+    return S, cell, f24, f53
+
+
+def accurate_tiles(cell, ng, m, log_tile):
+    """(first, last) tile of accurate mode's periodic tap window
+    [cell - m + 1, cell + m] (mod ng) with 2^log_tile-cell tiles."""
+    cell = np.asarray(cell, np.int64)
+    lo = cell - m + 1
+    hi = cell + m
+    lo = np.where(lo < 0, lo + ng, lo)
+    hi = np.where(hi >= ng, hi - ng, hi)
+    return lo >> log_tile, hi >> log_tile

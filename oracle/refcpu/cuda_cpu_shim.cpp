@@ -1,8 +1,9 @@
 /* Host implementation of the stand-in CUDA runtime / cuFFT used to run the
  * reference library's own sources on the CPU (golden-vector generation only).
  * Compiled by oracle/build_ref.py together with the reference's
- * src/gridding.cu, src/gaussian_filter.cu, src/cuna_kernel.cu and
- * src/cufft_utils.cu, once with -DDOUBLE_PRECISION and once without.
+ * src/gridding.cu, src/gaussian_filter.cu, src/cuna_kernel.cu,
+ * src/cufft_utils.cu, src/utils.cu and src/cuna.cpp, once with
+ * -DDOUBLE_PRECISION and once without.
  *
  * It also exports a small extern "C" surface (refcpu_*) so that Python can
  * drive the reference entry points through ctypes.
@@ -138,6 +139,9 @@ void cunfft_adjoint_raw_async_bootstrap(const dTyp *x, const dTyp *f_data, Compl
                                         const filter_properties *gpu_fprops,
                                         cudaStream_t stream, const unsigned int seed);
 
+/* copyResultsToCPU, src/cuna_kernel.cu:120-134 (no header declares it) */
+void copyResultsToCPU(plan *p);
+
 extern "C" {
 int refcpu_dtype_size(void) { return (int)sizeof(dTyp); }
 
@@ -186,6 +190,22 @@ void refcpu_adjoint_raw_async(const dTyp *x, const dTyp *y, Complex *f_hat, int 
   generate_filter_properties(x, n, ng, &h, &d);
   cunfft_adjoint_raw_async(x, y, f_hat, n, ng, d, (cudaStream_t)0);
   free_filter_properties(d, h);
+}
+
+/* init_plan (src/utils.cu:95-178) and cunfft_adjoint_from_plan
+ * (src/cuna_kernel.cu:137-145); the results are read back with
+ * copyResultsToCPU because from_plan never copies (its flag test at
+ * src/cuna_kernel.cu:142 is always false).  f_hat_win is filled when flags
+ * ask for the window function. */
+void refcpu_plan_adjoint(const dTyp *x, const dTyp *y, int n, int ng, unsigned flags, Complex *f_hat,
+                         Complex *f_hat_win) {
+  plan *p = (plan *)malloc(sizeof(plan));
+  init_plan(p, x, y, n, ng, flags);
+  cunfft_adjoint_from_plan(p);
+  copyResultsToCPU(p);
+  memcpy(f_hat, p->f_hat, sizeof(Complex) * ng);
+  if ((flags & CALCULATE_WINDOW_FUNCTION) && f_hat_win) memcpy(f_hat_win, p->f_hat_win, sizeof(Complex) * ng);
+  free_plan(p);
 }
 
 /* cunfft_adjoint_raw_async_bootstrap (src/cuna_kernel.cu:237) */

@@ -11,9 +11,19 @@ oracle.oracle.RefCPU:
     fast_gridding_bootstrap / cunfft_adjoint_raw_async_bootstrap for the
     bootstrap fixtures.
 
+and, in tests/golden/host/, the reference's host-side functions
+(src/utils.cu, src/cuna_kernel.cu:137-145):
+
+    host_utils.npz   scale_x on float and double arrays (sorted, unsorted,
+                     one and two elements, Julian dates) and nextPowerOfTwo
+                     on edge values
+    plan_*.npz       init_plan + cunfft_adjoint_from_plan, read back with
+                     copyResultsToCPU (f_hat and, with
+                     CALCULATE_WINDOW_FUNCTION, f_hat_win)
+
 Run where the reference source tree is available (the fixtures it writes
 are committed, so the tests need no reference tree):
-    python oracle/build_ref.py && python tests/golden/make_golden.py
+    python oracle/build_ref.py && python tests/golden/make_golden.py [--host-only]
 """
 import os
 import sys
@@ -91,15 +101,68 @@ def make_case(idx, name, prec, n, ng, kind, opt):
     return out
 
 
+HOST_DIR = os.path.join(HERE, "host")
+
+SCALE_X_INPUTS = [
+    [3.0, 4.0, 5.0, 7.0],
+    [-0.5, -0.1, 0.2, 0.5],
+    [0.0, 1.0],
+    [42.0],
+    [2451545.0, 2451545.25, 2451546.125, 2451600.0, 2451999.75],
+    [5.0, 1.0, 3.0, 2.0],
+]
+
+PLAN_CASES = [
+    # name, prec, n, ng, flags
+    ("plan_f32_n1000_ng2048", "f", 1000, 2048, 0),
+    ("plan_f32_window_n800_ng1024", "f", 800, 1024, 0x04),
+    ("plan_f64_n600_ng2048", "d", 600, 2048, 0x04),
+]
+
+
+def make_host():
+    os.makedirs(HOST_DIR, exist_ok=True)
+    out = {}
+    rng = np.random.default_rng(77)
+    inputs = SCALE_X_INPUTS + [list(np.sort(rng.uniform(0, 100, 257))), list(rng.normal(0, 3, 64))]
+    for prec, dt in (("f", np.float32), ("d", np.float64)):
+        R = RefCPU(prec)
+        for i, v in enumerate(inputs):
+            x = np.asarray(v, dt)
+            out["scale_x_%s_%d_in" % (prec, i)] = x
+            out["scale_x_%s_%d_out" % (prec, i)] = R.scale_x(x)
+    vals = np.array([0, 1, 2, 3, 4, 5, 7, 8, 9, 1000, 1023, 1024, 1025, 65535, 65536, 65537,
+                     2 ** 30, 2 ** 30 + 1, 2 ** 31 - 1, 2 ** 31, 2 ** 31 + 1, 2 ** 32 - 1], np.uint64)
+    out["next_pow2_in"] = vals.astype(np.uint32)
+    out["next_pow2_out"] = np.array([RefCPU("f").next_power_of_two(int(v)) for v in vals], np.uint32)
+    path = os.path.join(HOST_DIR, "host_utils.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", os.path.relpath(path), os.path.getsize(path), "bytes")
+    for idx, (name, prec, n, ng, flags) in enumerate(PLAN_CASES):
+        rng = np.random.default_rng(500 + idx)
+        dt = np.float32 if prec == "f" else np.float64
+        x = scaled_times(rng, n).astype(dt)
+        y = (np.sin(2 * np.pi * 7.0 * (x + 0.5)) + rng.normal(0, 0.3, n)).astype(dt)
+        f, w = RefCPU(prec).plan_adjoint(x, y, ng, flags)
+        rec = {"x": x, "y": y, "n": n, "ng": ng, "flags": flags, "f_hat": f}
+        if w is not None:
+            rec["f_hat_win"] = w
+        path = os.path.join(HOST_DIR, name + ".npz")
+        np.savez_compressed(path, **rec)
+        print("wrote", os.path.relpath(path), os.path.getsize(path), "bytes")
+
+
 def main():
     if not RefCPU.available("f") or not RefCPU.available("d"):
         if not build_ref.build(verbose=True):
             sys.exit("reference tree not available; cannot generate golden vectors")
-    for idx, (name, prec, n, ng, kind, opt) in enumerate(CASES):
-        out = make_case(idx, name, prec, n, ng, kind, opt)
-        path = os.path.join(HERE, name + ".npz")
-        np.savez_compressed(path, **out)
-        print("wrote", os.path.relpath(path), os.path.getsize(path), "bytes")
+    if "--host-only" not in sys.argv:
+        for idx, (name, prec, n, ng, kind, opt) in enumerate(CASES):
+            out = make_case(idx, name, prec, n, ng, kind, opt)
+            path = os.path.join(HERE, name + ".npz")
+            np.savez_compressed(path, **out)
+            print("wrote", os.path.relpath(path), os.path.getsize(path), "bytes")
+    make_host()
 
 
 if __name__ == "__main__":

@@ -248,3 +248,65 @@ def test_dropin_symbols(native_built, prec):
     xa, ya = np.ascontiguousarray(case["x"]), np.ascontiguousarray(case["y"])
     conv(xa.ctypes.data, ya.ctypes.data, out.ctypes.data, n, ng, 0)
     assert rel_l2(out, case["F"]) < _tol(dt)
+
+
+# ---------------------------------------------------------------------------
+# plans: init_plan + cunfft_adjoint_from_plan against the reference's own
+# src/utils.cu:95-178 and src/cuna_kernel.cu:137-145 (tests/golden/host)
+# ---------------------------------------------------------------------------
+class _Plan(ctypes.Structure):
+    """The reference's plan (inc/cuna_typedefs.h:118-149), 96 bytes."""
+    _fields_ = [("x_data", ctypes.c_void_p), ("f_data", ctypes.c_void_p), ("f_hat", ctypes.c_void_p),
+                ("f_hat_win", ctypes.c_void_p), ("g_f_hat", ctypes.c_void_p), ("g_f_hat_win", ctypes.c_void_p),
+                ("g_x_data", ctypes.c_void_p), ("g_f_data", ctypes.c_void_p), ("flags", ctypes.c_uint),
+                ("Ndata", ctypes.c_int), ("Ngrid", ctypes.c_int), ("filter_radius", ctypes.c_int),
+                ("fprops_host", ctypes.c_void_p), ("fprops_device", ctypes.c_void_p)]
+
+
+def _plan_cases():
+    import glob
+    import os
+    from conftest import GOLDEN_DIR
+    out = []
+    for f in sorted(glob.glob(os.path.join(GOLDEN_DIR, "host", "plan_*.npz"))):
+        d = dict(np.load(f))
+        d["name"] = os.path.basename(f)[:-4]
+        out.append(d)
+    return out
+
+
+@pytest.mark.parametrize("case", _plan_cases(), ids=lambda c: c["name"])
+def test_plan_from_reference_fixture(native_built, case):
+    """init_plan copies the host arrays in and builds the filter;
+    cunfft_adjoint_from_plan grids, transforms and normalises, and copies
+    f_hat (and f_hat_win with CALCULATE_WINDOW_FUNCTION) back to the plan's
+    host arrays -- which the reference means to do but never does (its flag
+    test is always false), so its results are read with copyResultsToCPU."""
+    from cunfft_adjoint_gb300 import _lib
+    assert ctypes.sizeof(_Plan) == 96
+    x, y = case["x"], case["y"]
+    prec = "f" if x.dtype == np.float32 else "d"
+    c = prec
+    lib = _lib.dropin(prec)
+    P, I = ctypes.c_void_p, ctypes.c_int
+    init = _sym(lib, "_Z9init_planP4planPK%sS2_iij" % c, [P, P, P, I, I, ctypes.c_uint])
+    run = _sym(lib, "_Z24cunfft_adjoint_from_planP4plan", [P])
+    free_plan = _sym(lib, "_Z9free_planP4plan", [P])
+    libc = ctypes.CDLL(None)
+    libc.malloc.restype = ctypes.c_void_p
+    libc.malloc.argtypes = [ctypes.c_size_t]
+    pp = libc.malloc(96)  # free_plan releases the plan itself, as the reference's does
+    n, ng, flags = int(case["n"]), int(case["ng"]), int(case["flags"])
+    xa, ya = np.ascontiguousarray(x), np.ascontiguousarray(y)
+    init(pp, xa.ctypes.data, ya.ctypes.data, n, ng, flags)
+    run(pp)
+    p = _Plan.from_address(pp)
+    assert (p.Ndata, p.Ngrid, p.flags) == (n, ng, flags)
+    ct = np.complex64 if prec == "f" else np.complex128
+    f_hat = np.ctypeslib.as_array((ctypes.c_byte * (ng * np.dtype(ct).itemsize)).from_address(p.f_hat)).view(ct)
+    tol = _tol(x.dtype)
+    assert rel_l2(f_hat.copy(), case["f_hat"]) < tol
+    if "f_hat_win" in case:
+        win = np.ctypeslib.as_array((ctypes.c_byte * (ng * np.dtype(ct).itemsize)).from_address(p.f_hat_win)).view(ct)
+        assert rel_l2(win.copy(), case["f_hat_win"]) < tol
+    free_plan(pp)

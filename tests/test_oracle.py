@@ -135,3 +135,65 @@ def test_cpu_pipeline_matches_oracle(oracle_lib):
     p = oracle_lib.CpuPipeline(len(case["x"]), ng)
     F = p.run(case["x"], case["y"])
     assert rel_l2(F, case["F"]) < 1e-5
+
+
+# ---------------------------------------------------------------------------
+# integer steps per sample (the checkers of the GPU's integer outputs)
+# ---------------------------------------------------------------------------
+
+def test_bulk_draws_match_scalar_draws(oracle_lib):
+    """The bulk draw restatement agrees with the per-draw one pinned above."""
+    assert np.array_equal(oracle_lib.bootstrap_draws_all(11, 37, 5).ravel(), oracle_lib.bootstrap_draws(11, 37, 5))
+    assert np.array_equal(oracle_lib.bootstrap_draws_all(0xFFFFFFF0, 3, 20).ravel(),
+                          oracle_lib.bootstrap_draws(0xFFFFFFF0, 3, 20))
+
+
+@pytest.mark.parametrize("case", PLAIN, ids=lambda c: c["name"])
+def test_taps_match_pinned_cells_and_filter(oracle_lib, case):
+    """compat_taps gives the cells of the pinned compat_cells, and its origin
+    u reproduces the golden E1/E2 of the reference's own sources:
+    eps = ng x - u lands in [R_f - 1, R_f + 1] for every in-range sample."""
+    x = case["x"]
+    ng = int(case["ng"])
+    dt = x.dtype
+    j, u, ms, me = oracle_lib.compat_taps(x, ng, dt, clamp=True)
+    assert np.array_equal(j, oracle_lib.compat_cells(x, ng, True))
+    rf = int(case["rf"])
+    inr = np.abs(x.astype(np.float64)) <= 0.5
+    eps = ng * x.astype(np.float64)[inr] - u[inr]
+    assert np.all((eps >= rf - 1) & (eps <= rf + 1))
+    has = ms < me
+    assert np.all(j[has].astype(np.int64) + ms[has] >= 0) and np.all(j[has].astype(np.int64) + me[has] <= ng)
+
+
+def test_tap_range_edges(oracle_lib):
+    """Tap ranges at the grid edges and for cells far outside it."""
+    ng = 64
+    x = np.array([-0.5, 0.5, 0.0, 2.0, -2.0, 1e9, -1e9, np.inf, -np.inf, np.nan], np.float32)
+    j, u, ms, me = oracle_lib.compat_taps(x, ng, np.float32, clamp=False)
+    assert (j[0], ms[0], me[0]) == (0, 0, 6)                 # taps 0..5 from cell 0
+    assert (j[1], ms[1], me[1]) == (63, -5, 1)               # taps -5..0 from the last cell
+    assert ms[3] == me[3] == 0 and ms[4] == me[4] == 0       # outside the grid: no taps
+    assert np.all(ms[5:9] == 0) and np.all(me[5:9] == 0)     # |j| > 2^30: no taps
+    assert j[9] == 0 and u[9] == 0                           # NaN converts to 0 as on the GPU
+
+
+def test_fixed_point_phase_against_rationals(oracle_lib):
+    """The fixed-point phase restatement against exact rational arithmetic:
+    S = frac((t - t0)/T) 2^64 to within the rounding of A = 2^64/T to 64
+    significant bits (relative 2^-63, so a few units times |t/T| + |t0/T|)
+    and the two truncations; the cell is floor(S ng / 2^64)."""
+    from fractions import Fraction
+    rng = np.random.default_rng(4)
+    for t0, T, ng in ((0.0, 3650.0, 1 << 22), (2451545.0, 1234.5678, 1 << 19), (17.25, 3.0, 3 << 20)):
+        t = np.concatenate([t0 + np.arange(-3, 4) * T, t0 + rng.integers(0, ng, 64) * (T / ng),
+                            t0 + rng.uniform(-5 * T, 5 * T, 64), [0.0, -0.0, 5e-324, -5e-324, 1e-300]])
+        S, cell, _, _ = oracle_lib.phases(t, t0, T, ng)
+        for ti, si, ci in zip(t, S, cell):
+            r = (Fraction(float(ti)) - Fraction(t0)) / Fraction(T)
+            exact = (r - (r.numerator // r.denominator)) * 2 ** 64
+            diff = (int(si) - int(exact)) % 2 ** 64
+            diff = min(diff, 2 ** 64 - diff)
+            bound = 4 * (abs(float(ti) / T) + abs(t0 / T)) + 4
+            assert diff <= bound, (ti, diff, bound)
+            assert ci == (int(si) * ng) >> 64
