@@ -352,6 +352,157 @@ def cpu_beside(wl, t, y, budget_s=1.5):
     return out
 
 
+def reference_cuda_leg(dev, steps, wl):
+    """The reference's OWN CUDA build (baseline/_ref, compiled for sm_103a by
+    oracle/build_ref_cuda.py from its sources with its Makefile's flags) on
+    the workload's inputs in the reference's units (x = t/T - 1/2, float,
+    ng = R*nf, its fixed filter radius 6), timed with CUDA events:
+
+    * as_is: cunfft_adjoint_raw_async as it ships, a cuFFT plan created and
+      destroyed inside every call (src/cuna_kernel.cu:188-232);
+    * kernels: its gridding and normalisation kernels (performGridding,
+      normalizeResults, src/cuna_kernel.cu:52-117) around one cuFFT C2C
+      inverse whose plan is made once -- the reference's arithmetic without
+      its per-call plan;
+    * bootstrap: cunfft_adjoint_raw_async_bootstrap, 1024 resamples of
+      N = 5000 on ng = 65536 (src/cuna_kernel.cu:236-289);
+
+    beside this library's drop-in entry points (cuna2_compat_adjoint_f32,
+    cuna2_compat_bootstrap_f32) on the same inputs, with the relative L2
+    difference of the two results."""
+    import ctypes
+    import platform
+    import torch
+    from cunfft_adjoint_gb300 import _lib
+    libdir = os.path.join(ROOT, "baseline", "_ref", "lib", platform.machine())
+    path = os.path.join(libdir, "libcunaf.so")
+    if not os.path.exists(path):
+        return {"unavailable": "the reference's CUDA build is not in baseline/_ref (oracle/build_ref_cuda.py)"}
+    ref = ctypes.CDLL(path, mode=ctypes.RTLD_LOCAL)
+    P, I = ctypes.c_void_p, ctypes.c_int
+    gen = ref._Z26generate_filter_propertiesPKfiiPP17filter_propertiesS3_
+    gen.argtypes, gen.restype = [P, I, I, P, P], None
+    raw = ref._Z24cunfft_adjoint_raw_asyncPKfS0_P6float2iiPK17filter_propertiesP11CUstream_st
+    raw.argtypes, raw.restype = [P, P, P, I, I, P, P], None
+    boot = ref._Z34cunfft_adjoint_raw_async_bootstrapPKfS0_P6float2iiiPK17filter_propertiesP11CUstream_stj
+    boot.argtypes, boot.restype = [P, P, P, I, I, I, P, P, ctypes.c_uint], None
+    init_plan = ref._Z9init_planP4planPKfS2_iij
+    init_plan.argtypes, init_plan.restype = [P, P, P, I, I, ctypes.c_uint], None
+    grid = ref._Z15performGriddingP4plan
+    norm = ref._Z16normalizeResultsP4plan
+    free_plan = ref._Z9free_planP4plan
+    for f in (grid, norm, free_plan):
+        f.argtypes, f.restype = [P], None
+    cufft = ctypes.CDLL("libcufft.so.12")
+    L = _lib.core()
+    n, nf, R, T = wl["n"], wl["nf"], wl["R"], wl["T"]
+    ng = R * nf
+    ts, ys = make_inputs(wl, 4242, 1)
+    x_h = (ts[0] / T - 0.5).astype(np.float32)
+    y_h = ys[0].astype(np.float32)
+    x = torch.as_tensor(x_h, device=dev)
+    y = torch.as_tensor(y_h, device=dev)
+    st = torch.cuda.default_stream(dev)  # the reference's kernels run on the legacy default stream
+    K = max(10, min(50, steps))
+
+    def timed(fn, k):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(k):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    with torch.cuda.stream(st):
+        h, d = P(), P()
+        gen(x.data_ptr(), n, ng, ctypes.byref(h), ctypes.byref(d))
+        f_ref = torch.zeros(ng, dtype=torch.complex64, device=dev)
+        raw(x.data_ptr(), y.data_ptr(), f_ref.data_ptr(), n, ng, d, None)
+        f_ref2 = torch.zeros(ng, dtype=torch.complex64, device=dev)
+        raw(x.data_ptr(), y.data_ptr(), f_ref2.data_ptr(), n, ng, d, None)
+        fp = _lib.FilterPropertiesF32()
+        E = [torch.empty(k, dtype=torch.float32, device=dev) for k in (n, n, 6)]
+        fp.E1, fp.E2, fp.E3 = E[0].data_ptr(), E[1].data_ptr(), E[2].data_ptr()
+        dfp = torch.zeros(ctypes.sizeof(fp), dtype=torch.uint8, device=dev)
+        _lib.check(L.cuna2_compat_filter_f32(x.data_ptr(), n, ng, ctypes.byref(fp), dfp.data_ptr(), None))
+        f_ours = torch.zeros(ng, dtype=torch.complex64, device=dev)
+        _lib.check(L.cuna2_compat_adjoint_f32(x.data_ptr(), y.data_ptr(), f_ours.data_ptr(), n, ng,
+                                              dfp.data_ptr(), None))
+        torch.cuda.synchronize()
+        a, b = f_ours.cpu().numpy().astype(np.complex128), f_ref.cpu().numpy().astype(np.complex128)
+        parity = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+        noise = float(np.linalg.norm(f_ref2.cpu().numpy().astype(np.complex128) - b) / np.linalg.norm(b))
+        del f_ref2
+        as_is = timed(lambda: raw(x.data_ptr(), y.data_ptr(), f_ref.data_ptr(), n, ng, d, None), K)
+        ours = timed(lambda: _lib.check(L.cuna2_compat_adjoint_f32(x.data_ptr(), y.data_ptr(), f_ours.data_ptr(),
+                                                                    n, ng, dfp.data_ptr(), None)), K)
+        # the reference's kernels around a cuFFT plan made once
+        libc = ctypes.CDLL(None)
+        libc.malloc.restype = P
+        libc.malloc.argtypes = [ctypes.c_size_t]
+        pp = libc.malloc(96)
+        init_plan(pp, x_h.ctypes.data, y_h.ctypes.data, n, ng, 0)
+        g_f_hat = ctypes.c_void_p.from_address(pp + 32).value
+        hplan = ctypes.c_int()
+        assert cufft.cufftPlan1d(ctypes.byref(hplan), ng, 0x29, 1) == 0  # CUFFT_C2C
+        exec_c2c = cufft.cufftExecC2C
+        exec_c2c.argtypes = [ctypes.c_int, P, P, I]
+
+        def kernels():
+            grid(pp)
+            exec_c2c(hplan.value, g_f_hat, g_f_hat, 1)  # CUFFT_INVERSE
+            norm(pp)
+
+        kern = timed(kernels, K)
+        cufft.cufftDestroy(hplan.value)
+        free_plan(pp)
+        # bootstrap: 1024 resamples of N = 5000 on ng = 65536
+        nb, nbs, ngb = 5000, 1024, 65536
+        rng = np.random.default_rng(77)
+        tb = rng.uniform(0, 100, nb)
+        xb = torch.as_tensor(((tb - tb.min()) / (tb.max() - tb.min()) - 0.5).astype(np.float32), device=dev)
+        yb = torch.as_tensor((np.sin(2 * np.pi * tb / 2.1) + rng.normal(0, 0.3, nb)).astype(np.float32), device=dev)
+        hb, db = P(), P()
+        gen(xb.data_ptr(), nb, ngb, ctypes.byref(hb), ctypes.byref(db))
+        fb_ref = torch.zeros(nbs * ngb, dtype=torch.complex64, device=dev)
+        boot(xb.data_ptr(), yb.data_ptr(), fb_ref.data_ptr(), nb, ngb, nbs, db, None, 7)
+        fpb = _lib.FilterPropertiesF32()
+        Eb = [torch.empty(k, dtype=torch.float32, device=dev) for k in (nb, nb, 6)]
+        fpb.E1, fpb.E2, fpb.E3 = Eb[0].data_ptr(), Eb[1].data_ptr(), Eb[2].data_ptr()
+        dfpb = torch.zeros(ctypes.sizeof(fpb), dtype=torch.uint8, device=dev)
+        _lib.check(L.cuna2_compat_filter_f32(xb.data_ptr(), nb, ngb, ctypes.byref(fpb), dfpb.data_ptr(), None))
+        fb_ours = torch.zeros(nbs * ngb, dtype=torch.complex64, device=dev)
+        _lib.check(L.cuna2_compat_bootstrap_f32(xb.data_ptr(), yb.data_ptr(), fb_ours.data_ptr(), nb, ngb, nbs,
+                                                dfpb.data_ptr(), 7, None))
+        torch.cuda.synchronize()
+        bpar = float(torch.linalg.vector_norm(fb_ours - fb_ref) / torch.linalg.vector_norm(fb_ref))
+        kb = max(5, min(20, steps))
+        b_ref = timed(lambda: boot(xb.data_ptr(), yb.data_ptr(), fb_ref.data_ptr(), nb, ngb, nbs, db, None, 7), kb)
+        b_ours = timed(lambda: _lib.check(L.cuna2_compat_bootstrap_f32(
+            xb.data_ptr(), yb.data_ptr(), fb_ours.data_ptr(), nb, ngb, nbs, dfpb.data_ptr(), 7, None)), kb)
+        del fb_ref, fb_ours
+    return {
+        "build": "reference sources compiled for sm_103a with its Makefile flags (--use_fast_math, -rdc, "
+                 "BLOCK_SIZE=256), cuFFT %s" % "12",
+        "workload": "%s; reference units: x = t/T - 1/2 (float32), ng = %d, filter radius 6" % (wl["name"], ng),
+        "as_is": {"ms_per_call": as_is, "value": 1000.0 / as_is, "unit": UNIT, "calls": K,
+                  "note": "cuFFT plan created and destroyed inside every call, as the reference does"},
+        "kernels": {"ms_per_call": kern, "value": 1000.0 / kern, "unit": UNIT, "calls": K,
+                    "note": "performGridding + cufftExecC2C (plan made once) + normalizeResults"},
+        "ours_dropin": {"ms_per_call": ours, "value": 1000.0 / ours, "unit": UNIT,
+                        "api": "cuna2_compat_adjoint_f32 (the drop-in's arithmetic)"},
+        "ours_over_as_is": as_is / ours, "ours_over_kernels": kern / ours,
+        "parity_rel_l2": parity, "reference_noise_floor": noise,
+        "bootstrap": {"resamples": nbs, "n": nb, "ng": ngb, "reference_ms_per_call": b_ref, "ours_ms_per_call": b_ours,
+                      "reference_resamples_per_s": nbs * 1000.0 / b_ref, "ours_resamples_per_s": nbs * 1000.0 / b_ours,
+                      "ours_over_reference": b_ref / b_ours, "parity_rel_l2": bpar},
+    }
+
+
 def dist_setup(backend):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -669,6 +820,8 @@ def main():
         f64 = {"value": 1000.0 / ms64, "unit": UNIT, "ms_per_step": ms64, "rel_err_vs_fp64_ndft": err64,
                "steps": k64}
 
+    r1 = reference_cuda_leg(dev, args.steps, wl) if rank == 0 and not args.no_side_legs else None
+
     batched = batched_legs(dev, args.steps) if rank == 0 and not args.no_side_legs else None
     if batched is not None:
         batched["autograd"] = autograd_leg(dev, args.steps)
@@ -713,6 +866,7 @@ def main():
             "gpu_launches": kernels_per_step * args.steps,
             "clocks": clk.summary(),
             "f64": f64,
+            "r1_reference_cuda": r1,
             "batched": batched,
             "cpu_baseline": cpu,
         }

@@ -52,12 +52,20 @@
 /* ------------------------------------------------------------------------ */
 
 /* C conversion (int)v of a double as the GPU performs it: truncation toward
- * zero, saturating at the int range, NaN -> 0 (PTX cvt.rzi.s32.f64). */
+ * zero, saturating at the int range.  A NaN double converts to INT_MIN
+ * (measured on sm_103a for the code nvcc emits for (int) of a double). */
 static int trunc_sat_int(double v) {
-  if (v != v) return 0;
+  if (v != v) return INT_MIN;
   if (v >= 2147483647.0) return INT_MAX;
   if (v <= -2147483648.0) return INT_MIN;
   return (int)v;
+}
+
+/* The same for a float source: saturating truncation, and a NaN float
+ * converts to 0 (measured on sm_103a for (int) of a float). */
+static int trunc_sat_int_f32(float v) {
+  if (v != v) return 0;
+  return trunc_sat_int((double)v);
 }
 
 /* wang_hash, src/gridding.cu:67-74 */
@@ -550,7 +558,7 @@ void cuna_oracle_compat_taps_f32(const float *x, int n, int ng, int clamp, int *
     int ms, me;
     compat_tap_range(j, ng, rf, &ms, &me);
     if (j_out) j_out[i] = j;
-    if (u_out) u_out[i] = trunc_sat_int((double)fmaf((float)ng, x[i], -(float)rf));
+    if (u_out) u_out[i] = trunc_sat_int_f32(fmaf((float)ng, x[i], -(float)rf));
     if (ms_out) ms_out[i] = ms;
     if (me_out) me_out[i] = me;
   }

@@ -192,6 +192,7 @@ def test_bootstrap_draws(L, oracle_lib, n, nbs, seed):
 # ---------------------------------------------------------------------------
 
 REC_F32 = np.dtype([("cell", "<i4"), ("a", "<u4"), ("b", "<u4"), ("p", "<i4")])
+REC_F32_VAL = np.dtype([("cell", "<i4"), ("a", "<u4"), ("b", "<u4"), ("p", "<u4")])  # p: the value's bits
 REC_F64 = np.dtype([("cell", "<i4"), ("p", "<i4"), ("a", "<u8"), ("b", "<u8"), ("v", "<u8")])
 
 
@@ -212,6 +213,8 @@ def _compat_bins_device(L, x, y, ng, boot):
                ctypes.byref(nrec), _stream()))
     torch.cuda.synchronize()
     R = recs.cpu().numpy()[:nrec.value * rdt.itemsize].view(rdt)
+    if dt == np.float32 and not boot:
+        R = R.view(REC_F32_VAL)
     E1 = fp.E1[:n].cpu().numpy().view(np.uint32 if dt == np.float32 else np.uint64)
     E2 = fp.E2[:n].cpu().numpy().view(np.uint32 if dt == np.float32 else np.uint64)
     return offs.cpu().numpy(), R, E1, E2
@@ -348,7 +351,7 @@ def test_accurate_phases(L, oracle_lib, case):
 def _plan_bins_device(L, plan, t, y, t0, T):
     n = len(t)
     td, yd = _dev(np.asarray(t, np.float64)), _dev(y)
-    lt, _ = plan.schedule()
+    lt, _ = plan.schedule
     ntiles = (plan.ng + (1 << lt) - 1) >> lt
     offs = torch.empty(ntiles + 1, dtype=torch.int32, device="cuda")
     rdt = REC_F32 if y.dtype == np.float32 else REC_F64
@@ -375,7 +378,7 @@ def test_accurate_binning(L, oracle_lib, case):
     tdt = torch.float32 if dt == np.float32 else torch.float64
     plan = nfft.AdjointNFFT(nf, R, m, tdt)
     if lt is not None:
-        plan.set_schedule(lt, plan.schedule()[1])
+        plan.set_schedule(lt, plan.schedule[1])
     ng = plan.ng
     if name == "large":
         t0, T, t = 0.0, 3650.0, large_t(seed=6, n=1_000_000 if dt == np.float32 else 300_000)

@@ -175,7 +175,9 @@ def test_tap_range_edges(oracle_lib):
     assert (j[1], ms[1], me[1]) == (63, -5, 1)               # taps -5..0 from the last cell
     assert ms[3] == me[3] == 0 and ms[4] == me[4] == 0       # outside the grid: no taps
     assert np.all(ms[5:9] == 0) and np.all(me[5:9] == 0)     # |j| > 2^30: no taps
-    assert j[9] == 0 and u[9] == 0                           # NaN converts to 0 as on the GPU
+    # NaN: the double cell converts to INT_MIN (no taps), the float origin
+    # to 0, as sm_103a converts them
+    assert j[9] == -2 ** 31 and u[9] == 0 and ms[9] == me[9] == 0
 
 
 def test_fixed_point_phase_against_rationals(oracle_lib):
