@@ -363,7 +363,10 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     const int mx = 200 * 1024;
     CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T, 4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_acc<T, 8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_acc_sg4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    CUNA_CK(cudaFuncSetAttribute(k_grid_acc_sg4<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_fixed<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     CUNA_CK(cudaFuncSetAttribute(k_grid_acc_seg<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
@@ -397,11 +400,17 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
     const T *wc = wts;
     const int64_t nv = n, sstr = p->ng;
     cudaError_t le;
+    const bool free_ = tail_free_gather(sizeof(T) == 4, p->m, p->tau) && !masked_gather_forced();
     if (p->grid_method == CUNA2_GRID_GATHER && cw8 && wts && group >= 2) {
       const size_t sm4 = grid_smem_bytes<T>(p->logTL, p->m, 4);
-      le = launch_pdl(k_grid_acc_sg4<T>, ggrid, gb, sm4, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+      if (free_) le = launch_pdl(k_grid_acc_sg4<T, false>, ggrid, gb, sm4, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+      else le = launch_pdl(k_grid_acc_sg4<T>, ggrid, gb, sm4, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
     } else if (p->grid_method == CUNA2_GRID_GATHER) {
-      if (cw8) le = launch_pdl(k_grid_acc<T, 8>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+      if (cw8 && free_)
+        le = launch_pdl(k_grid_acc<T, 8, false>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+      else if (cw8) le = launch_pdl(k_grid_acc<T, 8>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+      else if (free_)
+        le = launch_pdl(k_grid_acc<T, 4, false>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
       else le = launch_pdl(k_grid_acc<T, 4>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
     } else if (p->grid_method == CUNA2_GRID_FIXED) {
       le = launch_pdl(k_grid_fixed<T>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);

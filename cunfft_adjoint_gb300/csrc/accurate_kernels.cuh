@@ -338,24 +338,32 @@ __device__ __forceinline__ void gauss_cw(T y, T x, T k1, const GaussCW<T, CW> &g
 // reaches (0 <= rel - i < w2, w2 = 2m), by the centred factorisation of
 // gauss_cw; the mask is applied before the last product so that each tap is
 // one select and one fused multiply-add.
-template <typename T, int CW>
+// MASKED == false adds the record to all CW cells: cells outside its taps
+// lie more than m cells from it, where the Gaussian is below 2^(-k1 m^2) of
+// its peak; the plan takes this form only where that bound is negligible
+// (tail_free_gather), and then each tap is one product and one fused
+// multiply-add.
+template <typename T, int CW, bool MASKED = true>
 __device__ __forceinline__ void gauss_acc(T y, T x, T k1, const GaussCW<T, CW> &g, int rel, int w2, T *a) {
   constexpr int H = CW / 2;
   const T xc = x + (T)H;
   const T E = y * exp2_g(-k1 * xc * xc);
   const T Q = exp2_g((T)(-2) * k1 * xc), Qi = exp2_g((T)2 * k1 * xc);
-  a[H] += (unsigned)(rel - H) < (unsigned)w2 ? E : (T)0;
+  if (MASKED) a[H] += (unsigned)(rel - H) < (unsigned)w2 ? E : (T)0;
+  else a[H] += E;
   T u = E;
 #pragma unroll
   for (int j = 1; j < CW - H; ++j) {
     u *= Q;
-    a[H + j] = fma((unsigned)(rel - H - j) < (unsigned)w2 ? u : (T)0, g.c[j], a[H + j]);
+    if (MASKED) a[H + j] = fma((unsigned)(rel - H - j) < (unsigned)w2 ? u : (T)0, g.c[j], a[H + j]);
+    else a[H + j] = fma(u, g.c[j], a[H + j]);
   }
   u = E;
 #pragma unroll
   for (int j = 1; j <= H; ++j) {
     u *= Qi;
-    a[H - j] = fma((unsigned)(rel - H + j) < (unsigned)w2 ? u : (T)0, g.c[j], a[H - j]);
+    if (MASKED) a[H - j] = fma((unsigned)(rel - H + j) < (unsigned)w2 ? u : (T)0, g.c[j], a[H - j]);
+    else a[H - j] = fma(u, g.c[j], a[H - j]);
   }
 }
 
@@ -386,7 +394,7 @@ __device__ __forceinline__ void grid_slots(int p0, int ng, int TL, int m, int &s
 // SG > 1 (slab weights given, CW = 8 on 2048-cell tiles): SG slabs share each
 // record's Gaussian, computed once per record visit and scaled by each slab's
 // value from shared memory.
-template <typename T, int CW, class Src, int SG = 1>
+template <typename T, int CW, class Src, int SG = 1, bool MASKED = true>
 __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
                                                int base, T *__restrict__ grid, const AccParams<T> &e,
                                                const T *__restrict__ wts, int64_t nvals, int sbeg, int send,
@@ -493,7 +501,7 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
             r.f = rc[u].a;
             r.y = rc[u].b;
             r.lc = lc;
-            r.pad = 0;
+            r.pad = __float_as_int((float)lc);  // the slot as a float (exact), for the unmasked gather
             srec[pos] = r;
             sp[pos] = rc[u].p;
           }
@@ -530,17 +538,24 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
 #pragma unroll
         for (int i = 0; i < CW; ++i) a[0][i] = (T)0;
         const int ctr = cl0 + m, w2 = 2 * m;
+        const float ctrf = (float)ctr;
         for (int r = rb; r < re; ++r) {
           const SRec<T> rr = srec[r];
-          const int rel = rr.lc - cl0;            // lc - c for c = cl0
-          const T dd0 = (T)(ctr - rr.lc) - rr.f;  // d - f for c = cl0
+          const int rel = rr.lc - cl0;  // lc - c for c = cl0
+          // d - f for c = cl0; unmasked float tiles take the slot as a float
+          // (a difference of small integers, exact) and skip the conversion
+          T dd0;
+          if constexpr (!MASKED && sizeof(T) == 4) dd0 = (ctrf - __int_as_float(rr.pad)) - rr.f;
+          else dd0 = (T)(ctr - rr.lc) - rr.f;
           if constexpr (SG == 1) {
-            gauss_acc<T, CW>(rr.y, dd0, e.k1, gw, rel, w2, a[0]);
+            gauss_acc<T, CW, MASKED>(rr.y, dd0, e.k1, gw, rel, w2, a[0]);
           } else {
             T w[CW];
             gauss_cw<T, CW>((T)1, dd0, e.k1, gw, w);
+            if constexpr (MASKED) {
 #pragma unroll
-            for (int i = 0; i < CW; ++i) w[i] = (unsigned)(rel - i) < (unsigned)w2 ? w[i] : (T)0;
+              for (int i = 0; i < CW; ++i) w[i] = (unsigned)(rel - i) < (unsigned)w2 ? w[i] : (T)0;
+            }
 #pragma unroll
             for (int g = 0; g < SG; ++g) {
               const T yg = yv[g * CAP + r];
@@ -577,7 +592,7 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
 }
 
 // slab groups sharing each record's Gaussian (bootstrap resamples, channels)
-template <typename T>
+template <typename T, bool MASKED = true>
 __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 3 : 2) k_grid_acc_sg4(
     const typename RecOf<T>::type *recs, const int *off, T *grid, AccParams<T> e, const T *wts, int64_t nvals,
     int nslab, int group, int64_t slab_stride) {
@@ -588,13 +603,13 @@ __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 3 : 2) k_grid_a
   const CgSrc<typename RecOf<T>::type> rp{recs};
   const int r0 = __ldcg(off + tile), r1 = __ldcg(off + tile + 1);
   if constexpr (sizeof(T) == 4)
-    grid_tile_body<T, 8, CgSrc<typename RecOf<T>::type>, 4>(rp, r0, r1, tile << e.logTL, grid, e, wts, nvals, sbeg,
-                                                             send, slab_stride);
+    grid_tile_body<T, 8, CgSrc<typename RecOf<T>::type>, 4, MASKED>(rp, r0, r1, tile << e.logTL, grid, e, wts, nvals,
+                                                                     sbeg, send, slab_stride);
   else  // double plans keep one slab per pass (four accumulator sets do not fit)
     grid_tile_body<T, 8>(rp, r0, r1, tile << e.logTL, grid, e, wts, nvals, sbeg, send, slab_stride);
 }
 
-template <typename T, int CW>
+template <typename T, int CW, bool MASKED = true>
 __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 4 : 2) k_grid_acc(
     const typename RecOf<T>::type *recs, const int *off, T *grid, AccParams<T> e, const T *wts, int64_t nvals,
     int nslab, int group, int64_t slab_stride) {
@@ -604,8 +619,19 @@ __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 4 : 2) k_grid_a
   const int tile = blockIdx.x;
   const int sbeg = blockIdx.y * group, send = min(nslab, sbeg + group);
   const CgSrc<typename RecOf<T>::type> rp{recs};
-  grid_tile_body<T, CW>(rp, __ldcg(off + tile), __ldcg(off + tile + 1), tile << e.logTL, grid, e, wts, nvals, sbeg,
-                        send, slab_stride);
+  grid_tile_body<T, CW, CgSrc<typename RecOf<T>::type>, 1, MASKED>(rp, __ldcg(off + tile), __ldcg(off + tile + 1),
+                                                                    tile << e.logTL, grid, e, wts, nvals, sbeg, send,
+                                                                    slab_stride);
+}
+
+// Whether a float plan's gather may add each record to whole cell groups
+// without the tap masks: every cell beyond a record's taps lies more than m
+// cells from it, where the Gaussian exp(-d^2 / (4 tau)) is below
+// exp(-m^2 / (4 tau)); below 1e-8 of the peak (under float rounding) the
+// extra terms only bring the kernel closer to the untruncated Gaussian that
+// the deconvolution divides by.  Double plans keep the masks.
+inline bool tail_free_gather(bool is_float, int m, double tau) {
+  return is_float && (double)m * m / (4.0 * tau) >= 18.43;  // exp(-18.43) = 1e-8
 }
 
 // Scatter form of the same tile gridding: the tile's cells accumulate in

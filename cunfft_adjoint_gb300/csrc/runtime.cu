@@ -231,6 +231,14 @@ bool pdl_enabled() {
   return on;
 }
 
+bool masked_gather_forced() {
+  static const bool on = [] {
+    const char *v = getenv("CUNA2_GATHER_MASKS");
+    return v && v[0] == '1';
+  }();
+  return on;
+}
+
 bool tma_enabled() {
   static const bool on = [] {
     const char *v = getenv("CUNA2_TMA");

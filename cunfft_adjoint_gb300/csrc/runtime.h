@@ -75,6 +75,9 @@ int *wait_timeout_counter();
 // for 1024 grids of 2^15 points) where the pass streams from HBM, because a
 // CTA can start its transform only once all its boxes have landed.
 bool tma_enabled();
+// CUNA2_GATHER_MASKS=1: float plans keep the tap masks in the gather even
+// where the Gaussian's tail allows the unmasked form (for comparisons)
+bool masked_gather_forced();
 // Tiled 3D tensor map (CUtensorMap, 128 bytes at `map`) over float32 data at
 // `base`: dims {d0, d1, d2} (d0 innermost), byte strides {s1, s2} of
 // dimensions 1 and 2, box {b0, b1, 1}.  Returns false when the CUDA driver entry

@@ -424,3 +424,44 @@ def test_graph_replay_on_streams_matches_eager(nfft):
         torch.cuda.synchronize()
         for k in range(3):
             assert np.array_equal(outs[k].cpu().numpy(), ref[(k + rnd) % 3]), (rnd, k)
+
+
+_GATHER_SCRIPT = r"""
+import sys
+import numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+from cunfft_adjoint_gb300 import nfft, _lib
+rng = np.random.default_rng(21)
+out = {}
+for (n, nf, R, m) in ((200_000, 1 << 18, 4, 12), (150_000, 1 << 16, 2, 8), (40_000, 1 << 15, 2, 5)):
+    t = torch.as_tensor(rng.uniform(0, 300.0, n), device="cuda")
+    y = torch.as_tensor(rng.normal(0, 1, n).astype(np.float32), device="cuda")
+    plan = nfft.AdjointNFFT(nf, R, m, torch.float32)
+    plan.set_schedule(11, _lib.GRID_GATHER)
+    out["F_%d_%d" % (R, m)] = plan(t, y, 0.0, 300.0).cpu().numpy()
+    out["B_%d_%d" % (R, m)] = plan.bootstrap(t[:5000], y[:5000], 16, 3, 0.0, 300.0).cpu().numpy()
+np.savez(sys.argv[2], **out)
+"""
+
+
+def test_unmasked_gather_matches_masked(tmp_path):
+    """Float plans whose Gaussian is below 1e-8 of its peak beyond m cells
+    (m = 12, R = 4 and m = 8, R = 2 here) grid each record into whole cell
+    groups without the tap masks; the spectra agree with the masked form
+    (CUNA2_GATHER_MASKS=1) to float rounding.  m = 5, R = 2 keeps the masks
+    in both runs (only the order of records within a cell, which follows the
+    shared-memory atomics, can differ)."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    script = tmp_path / "gather.py"
+    script.write_text(_GATHER_SCRIPT)
+    res = {}
+    for tag, env in (("masked", {"CUNA2_GATHER_MASKS": "1"}), ("free", {"CUNA2_GATHER_MASKS": "0"})):
+        r = subprocess.run([sys.executable, str(script), root, str(tmp_path / (tag + ".npz"))],
+                           env={**os.environ, **env}, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        res[tag] = np.load(tmp_path / (tag + ".npz"))
+    for key in res["masked"].files:
+        assert rel_l2(res["free"][key], res["masked"][key]) < 1e-6, key
