@@ -265,11 +265,13 @@ template <typename T> struct SampAccS {
 // Gridding, gather form.  One CTA owns tile [base, base + TL) of the grid and
 // the records binned to it (its own samples plus the halo samples within m
 // cells of its edges).  Per chunk of at most CAP records it counting-sorts
-// them in shared memory by local slot lc = cell - base + m (integer atomics
-// only), then every thread sums, for each of its cells c, the samples whose
-// slot lies in [c - base, c - base + 2m): w = y exp(-(d - f)^2 / (4 tau)),
-// d = c - cell.  Partial sums stay in registers across chunks and are written
-// once, coalesced.  No floating-point atomics.
+// them in shared memory by group of CW consecutive local slots (slot lc =
+// cell - base + m; integer atomics only), then every thread sums, for each
+// of its CW cells c, the records of the groups covering slots [c - base,
+// c - base + 2m): w = y exp(-(d - f)^2 / (4 tau)), d = c - cell (records of
+// those groups outside the window are masked, or, in the unmasked form, add
+// their negligible tail).  Partial sums stay in registers across chunks and
+// are written once, coalesced.  No floating-point atomics.
 // ---------------------------------------------------------------------------
 template <typename T> struct GridCfg;
 template <> struct GridCfg<float> { static constexpr int CAP = 1024; };
@@ -407,8 +409,11 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
   constexpr int RPT = CAP / kGridThreads;  // records per thread per chunk
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int TL = 1 << e.logTL, m = e.m, W = TL + 2 * m;
+  // records are counting-sorted into groups of CW consecutive slots (slot =
+  // local cell + m), the unit of a thread's cell group: NG + 1 counters
+  const int NG = (W + CW - 1) / CW;
   const int ng = (int)e.ng;
-  int *start = reinterpret_cast<int *>(smem_raw);                                       // W + 1 slots
+  int *start = reinterpret_cast<int *>(smem_raw);                                       // NG + 1 groups
   SRec<T> *srec = reinterpret_cast<SRec<T> *>(smem_raw + sizeof(int) * ((W + 2 + 3) & ~3));  // placed records
   int *sp = reinterpret_cast<int *>(srec + CAP);                                         // sample index
   T *yv = reinterpret_cast<T *>(sp + CAP);  // SG > 1: yv[s * CAP + r], value of slab s for placed record r
@@ -431,7 +436,7 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
       const int c0 = r0 + ck * chunk;
       const int cnt = min(chunk, r1 - c0);
       if (nchunks > 1 || slab == sbeg) {
-        for (int i = threadIdx.x; i <= W; i += kGridThreads) start[i] = 0;
+        for (int i = threadIdx.x; i <= NG; i += kGridThreads) start[i] = 0;
         __syncthreads();
         // load this thread's records; each maps to up to two slots (two only
         // when the tile wraps onto itself, i.e. one tile spans the whole grid)
@@ -447,15 +452,15 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
           if (i < cnt) {
             int s0, s1;
             grid_slots(rc[u].cell - base, ng, TL, m, s0, s1);
-            if (s0 >= 0) atomicAdd(&start[s0], 1);
-            if (s1 >= 0) atomicAdd(&start[s1], 1);
+            if (s0 >= 0) atomicAdd(&start[s0 / CW], 1);
+            if (s1 >= 0) atomicAdd(&start[s1 / CW], 1);
           }
         }
         __syncthreads();
-        // exclusive scan of start[0..W]: slot lc occupies [start[lc], start[lc+1])
+        // exclusive scan of start[0..NG]: group g occupies [start[g], start[g+1])
         {
-          const int per = (W + 1 + kGridThreads - 1) / kGridThreads;
-          const int b0 = min((int)threadIdx.x * per, W + 1), b1 = min(b0 + per, W + 1);
+          const int per = (NG + 1 + kGridThreads - 1) / kGridThreads;
+          const int b0 = min((int)threadIdx.x * per, NG + 1), b1 = min(b0 + per, NG + 1);
           int sum = 0;
           for (int i = b0; i < b1; ++i) sum += start[i];
           const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -485,7 +490,7 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
           }
         }
         __syncthreads();
-        // place: afterwards start[lc] is the END of slot lc
+        // place: afterwards start[g] is the END of group g
 #pragma unroll
         for (int u = 0; u < RPT; ++u) {
           const int i = threadIdx.x + u * kGridThreads;
@@ -496,7 +501,7 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
           for (int q = 0; q < 2; ++q) {
             const int lc = sl[q];
             if (lc < 0) continue;
-            const int pos = atomicAdd(&start[lc], 1);
+            const int pos = atomicAdd(&start[lc / CW], 1);
             SRec<T> r;
             r.f = rc[u].a;
             r.y = rc[u].b;
@@ -509,13 +514,13 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
         __syncthreads();
       }
       if (SG == 1 && wts) {  // this slab's values for the placed records
-        const int placed = start[W - 1];
+        const int placed = start[(W - 1) / CW];
         const T *ws = wts + (int64_t)slab * nvals;
         for (int i = threadIdx.x; i < placed; i += kGridThreads) srec[i].y = ws[sp[i]];
         __syncthreads();
       }
       if constexpr (SG > 1) {  // the group's values (0 past the last slab)
-        const int placed = start[W - 1];
+        const int placed = start[(W - 1) / CW];
 #pragma unroll
         for (int g = 0; g < SG; ++g) {
           const T *ws = wts + (int64_t)(slab + g) * nvals;
@@ -531,8 +536,13 @@ __device__ __forceinline__ void grid_tile_body(const Src &recs, int r0, int r1,
       for (int q = 0; q < MAXC / CW; ++q) {
         const int cl0 = (threadIdx.x + q * kGridThreads) * CW;
         if (q >= npass || cl0 >= TL) continue;
-        const int rb = cl0 == 0 ? 0 : start[cl0 - 1];
-        const int re = start[cl0 + CW - 1 + 2 * m - 1];
+        // the groups holding slots cl0 .. cl0 + CW + 2m - 2 (cl0 is a
+        // multiple of CW; the last group may hold up to CW - 1 slots beyond
+        // the window, whose records the masks drop or, unmasked, add below
+        // 2^(-k1 m^2))
+        const int g0 = cl0 / CW, g1 = (cl0 + CW + 2 * m - 2) / CW;
+        const int rb = g0 == 0 ? 0 : start[g0 - 1];
+        const int re = start[g1];
         // SG > 1 has one pass (CW = MAXC = 8) and accumulates into acc directly
         T a[1][CW];
 #pragma unroll
