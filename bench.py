@@ -177,8 +177,12 @@ def batched_legs(dev, steps, which=("bootstrap", "uneven"), plain=True):
         F = torch.empty((nbs, nf), dtype=torch.complex64, device=dev)
         for i in range(3):
             plan.bootstrap(td, yd, nbs, i, 0.0, 100.0, out=F)
+        # one CUDA graph replayed for every call, its draw seed updated per call
+        plan.set_graph(True)
+        for i in range(3):
+            plan.bootstrap(td, yd, nbs, 100 + i, 0.0, 100.0, out=F)
         torch.cuda.synchronize()
-        k = max(3, min(20, steps // 50))
+        k = max(20, min(200, steps // 10))
         e0.record()
         for i in range(k):
             plan.bootstrap(td, yd, nbs, i, 0.0, 100.0, out=F)
@@ -186,11 +190,13 @@ def batched_legs(dev, steps, which=("bootstrap", "uneven"), plain=True):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / k
         out["bootstrap"] = {"workload": "N=5000, 1024 resamples, Nf=32768, R=2, m=8", "value": nbs * 1000.0 / ms,
-                            "unit": UNIT, "ms_per_call": ms, "calls": k}
+                            "unit": UNIT, "ms_per_call": ms, "calls": k,
+                            "graph": "one captured graph per argument set, a new draw seed every call"}
         if plain:
             # plain per-resample path: one single-series transform per resample
             # (resampled inputs prepared outside the timed region)
-            draws = [rng.integers(0, n, n) for _ in range(64)]
+            plan.set_graph(False)  # eager single-series calls, one per resample
+            draws = [rng.integers(0, n, n) for _ in range(max(64, min(256, steps // 8)))]
             tds = [td[torch.as_tensor(d, device=dev)] for d in draws]
             yds = [yd[torch.as_tensor(d, device=dev)] for d in draws]
             Fp = torch.empty(nf, dtype=torch.complex64, device=dev)
@@ -217,11 +223,13 @@ def batched_legs(dev, steps, which=("bootstrap", "uneven"), plain=True):
         yy = rng.normal(0, 1, int(nser.sum())).astype(np.float32)
         bp = BatchAdjointNFFT(nser, nfs, 2, 8, np.zeros(ns), Ts, torch.float32, device=dev, graph=True)
         tdd, ydd = torch.as_tensor(tt, device=dev), torch.as_tensor(yy, device=dev)
+        # the batch's own autotuner picks the tile size and gridding form
+        blt, bgm, _ = bp.autotune(tdd, ydd, reps=3)
         FF = torch.empty(int(nfs.sum()), dtype=torch.complex64, device=dev)
         for i in range(3):
             bp(tdd, ydd, out=FF)
         torch.cuda.synchronize()
-        k = max(3, min(10, steps // 100))
+        k = max(20, min(100, steps // 20))
         e0.record()
         for i in range(k):
             bp(tdd, ydd, out=FF)
@@ -229,7 +237,9 @@ def batched_legs(dev, steps, which=("bootstrap", "uneven"), plain=True):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / k
         out["uneven"] = {"workload": "4096 series, N log-U[100,1e5] (total %d), Nf=nextpow2(4N)<=2^18, R=2, m=8"
-                         % int(nser.sum()), "value": ns * 1000.0 / ms, "unit": UNIT, "ms_per_call": ms, "calls": k}
+                         % int(nser.sum()), "value": ns * 1000.0 / ms, "unit": UNIT, "ms_per_call": ms, "calls": k,
+                         "schedule": {"log_tile": blt, "grid_method": ["gather", "scatter", "fixed"][bgm]},
+                         "graph": True}
         if not plain:
             return out
         # plain per-series path: one single-series plan call per series (plans
@@ -278,7 +288,7 @@ def autograd_leg(dev, steps):
     for _ in range(3):
         step()
     torch.cuda.synchronize()
-    k = max(3, min(20, steps // 100))
+    k = max(20, min(100, steps // 20))
     a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a0.record()
     for _ in range(k):
@@ -286,8 +296,32 @@ def autograd_leg(dev, steps):
     a1.record()
     torch.cuda.synchronize()
     ms = a0.elapsed_time(a1) / k
+    # plain per-series path: the single-series differentiable function, one
+    # forward and one backward per series
+    from cunfft_adjoint_gb300.autograd import adjoint_nfft
+    from cunfft_adjoint_gb300.nfft import AdjointNFFT
+    plan = AdjointNFFT(nf, 2, 10, torch.float32, device=dev)
+
+    def plain_step():
+        for b in range(B):
+            tb, yb = t[b].detach().requires_grad_(True), y[b].detach().requires_grad_(True)
+            F = adjoint_nfft(tb, yb, plan, 0.0, T)
+            (w[b] * (F.real ** 2 + F.imag ** 2)).sum().backward()
+
+    plain_step()
+    torch.cuda.synchronize()
+    kp = max(3, min(10, steps // 200))
+    a0.record()
+    for _ in range(kp):
+        plain_step()
+    a1.record()
+    torch.cuda.synchronize()
+    msp = a0.elapsed_time(a1) / kp
     return {"workload": "64 series x N=2e5, Nf=2^18, R=2, m=10, loss sum w|F|^2, forward + backward (t, y)",
-            "value": B * 1000.0 / ms, "unit": "series/s (forward+backward)", "ms_per_batch": ms, "steps": k}
+            "value": B * 1000.0 / ms, "unit": "series/s (forward+backward)", "ms_per_batch": ms, "steps": k,
+            "plain_value": B * 1000.0 / msp, "plain_ms_per_batch": msp, "plain_steps": kp,
+            "batched_over_plain": msp / ms,
+            "plain": "per series: the single-series autograd function, one forward and one backward"}
 
 
 def cpu_baseline(wl, budget_s=20.0):
@@ -667,27 +701,43 @@ def main():
     value = replica_value(ms, args.steps, ws)
     ms1 = timed(1, args.steps) / args.steps  # one stream: the per-transform latency
 
-    # per-launch durations (CUDA events between launches on the plan's stream)
+    # per-launch durations: cuna2_plan_profile replays the transform as a CUDA
+    # graph with an event node after every launch (launches serialised), so
+    # each duration is one kernel's, timed on the device; a 512 MB read ahead
+    # of each replay evicts the inputs from L2, as in the timed loop
     import ctypes
     stage_ms = (ctypes.c_float * 16)()
     names = (ctypes.c_char_p * 16)()
     nst = ctypes.c_int()
     acc = {}
     reps = 10
-    # a 256 MB read ahead of each profiled transform keeps the device busy
-    # while the host enqueues the launches (so the marks time the kernels,
-    # not the host) and evicts the inputs from L2, as in the timed loop; a
-    # read leaves no dirty lines to be written back during the marks
-    busy = torch.zeros(64 << 20, dtype=torch.float32, device=dev)
+    evict = torch.zeros(128 << 20, dtype=torch.float32, device=dev)
     for r in range(reps):
         s = (r * 5) % nsets
         with torch.cuda.stream(stream):
-            busy.sum()
+            evict.sum()
         _lib.check(L.cuna2_plan_profile(plan._h, td[s].data_ptr(), yd[s].data_ptr(), Fd[0].data_ptr(), n, 0.0, T,
                                         stream.cuda_stream or None, stage_ms, names, 16, ctypes.byref(nst)))
         for i in range(nst.value):
             acc.setdefault(names[i].decode(), []).append(stage_ms[i])
-    stages = {k: float(np.mean(v)) for k, v in acc.items()}
+    stages = {k: float(np.median(v)) for k, v in acc.items()}
+    # every profiled interval includes one event node's gap: take it out
+    gap = stages.pop("event_gap", 0.0)
+    stages = {k: max(v - gap, 0.0) for k, v in stages.items()}
+    # the gridding kernel's own launch time (the roofline's kernel): one
+    # transform in which the gridding launch repeats back to back between two
+    # events on the plan's stream, on the records of that transform
+    gms = ctypes.c_float()
+    grid_runs = []
+    for r in range(5):
+        s = (r * 3) % nsets
+        with torch.cuda.stream(stream):
+            evict.sum()
+        _lib.check(L.cuna2_plan_time_grid(plan._h, td[s].data_ptr(), yd[s].data_ptr(), Fd[0].data_ptr(), n, 0.0, T,
+                                          50, stream.cuda_stream or None, ctypes.byref(gms)))
+        grid_runs.append(gms.value)
+    grid_ms = float(np.median(grid_runs))
+    del evict
 
     # comparator: cuFFT's real-to-complex transform of the same ng-point real
     # grid (torch.fft.rfft), L2-resident like the grid our two passes work on;
@@ -707,9 +757,9 @@ def main():
                "points": ng, "note": "cuFFT R2C alone; ours includes unpack, deconvolution and centring"}
     del g_real
     sb = stage_bytes(n, ng, nf)
-    dom = max(stages, key=stages.get)
+    dom = "grid"  # the largest share of the transform in the launch lists (profiles/)
     peak, peak_kind = peaks()
-    ach = sb.get(dom, 0) / (stages[dom] * 1e-3) / 1e9
+    ach = sb.get(dom, 0) / (grid_ms * 1e-3) / 1e9
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic_large.json")
     if os.path.exists(tfile):
@@ -845,10 +895,17 @@ def main():
                                     "grid_method": ["gather", "scatter", "fixed"][schedule[1]]}},
             "rel_err_vs_fp64_ndft": err,
             "single_stream": {"value": ws * 1000.0 / ms1, "ms_per_step": ms1},
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
-                         "traffic": traffic, "algorithmic_bytes": sb.get(dom, 0)},
+            "roofline": {"bound": "hbm", "kernel": "grid (k_grid_acc, gather gridding)", "achieved": ach,
+                         "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
+                         "traffic": traffic, "algorithmic_bytes": sb.get(dom, 0),
+                         "kernel_ms": grid_ms,
+                         "timing": "mean of 50 back-to-back launches of the gridding kernel on one transform's "
+                                   "records, CUDA events on the plan's stream (cuna2_plan_time_grid), median of 5"},
             "stages_ms": stages,
+            "stages_note": "per-launch device time, launches serialised (graph replay with an event after each "
+                           "launch, the event nodes' own gap of %.4f ms taken out); the timed step overlaps "
+                           "launches (dependent launch) and streams, so the stages sum to more than "
+                           "ms_per_step" % gap,
             "pipeline_gbs": total_bytes / (ms_step * 1e-3) / 1e9,
             # compulsory traffic only: t and y in, the spectrum out
             "compulsory_gbs": (n * 12 + nf * 8) / (ms_step * 1e-3) / 1e9,

@@ -71,6 +71,7 @@ CORE_SIGNATURES = {
     "cuna2_adjoint_host_async": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P]),
     "cuna2_adjoint_bootstrap": (_I, [_P, _P, _P, _P, _I64, _I, _U, _D, _D, _P]),
     "cuna2_adjoint_backward": (_I, [_P, _P, _P, _P, _P, _P, _I64, _D, _D, _P]),
+    "cuna2_adjoint_backward_batch": (_I, [_P, _P, _P, _P, _P, _P, _I64, _I, _P, _P, _P]),
     "cuna2_adjoint_multi": (_I, [_P, _P, _P, _P, _I64, _I, _D, _D, _P]),
     "cuna2_lomb_scargle": (_I, [_I, _P, _P, _P, _I64, _I64, _D, _D, _I, _I, _P, _P]),
     "cuna2_plan_set_graph": (_I, [_P, _I]),
@@ -81,12 +82,16 @@ CORE_SIGNATURES = {
     "cuna2_plan_get_schedule": (_I, [_P, _P, _P]),
     "cuna2_plan_autotune": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P, _I, _P]),
     "cuna2_plan_profile": (_I, [_P, _P, _P, _P, _I64, _D, _D, _P, _P, _P, _I, _P]),
+    "cuna2_plan_time_grid": (_I, [_P, _P, _P, _P, _I64, _D, _D, _I, _P, _P]),
     "cuna2_batch_plan_create": (_I, [_P, _I, _I, _P, _P, _I, _I, _P, _P]),
     "cuna2_batch_plan_destroy": (_I, [_P]),
     "cuna2_batch_set_times": (_I, [_P, _P, _P]),
     "cuna2_batch_info": (_I, [_P, _P, _P]),
     "cuna2_batch_set_graph": (_I, [_P, _I]),
     "cuna2_batch_adjoint": (_I, [_P, _P, _P, _P, _P]),
+    "cuna2_batch_set_schedule": (_I, [_P, _I, _I]),
+    "cuna2_batch_get_schedule": (_I, [_P, _P, _P]),
+    "cuna2_batch_autotune": (_I, [_P, _P, _P, _P, _P, _I, _P]),
     "cuna2_inspect_compat_taps_f32": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P]),
     "cuna2_inspect_compat_taps_f64": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P]),
     "cuna2_inspect_bootstrap_draws": (_I, [_I, _I, _U, _P, _P]),

@@ -48,15 +48,8 @@ class _BatchFunction(torch.autograd.Function):
         t, y = ctx.saved_tensors
         op = ctx.op
         need_t, need_y = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
-        gt = torch.empty_like(t) if need_t else None
-        gy = torch.empty_like(y) if need_y else None
-        g = grad_F.contiguous()
-        for b in range(op.B):  # one hand-written VJP per series, stream-ordered
-            gyb, gtb = op.plan.backward(t[b].detach(), y[b].detach(), g[b], op.t0[b], op.T[b], need_y, need_t)
-            if need_t:
-                gt[b] = gtb
-            if need_y:
-                gy[b] = gyb
+        # all series' vector-Jacobian products in one batched execution
+        gy, gt = op.plan.backward_batch(t.detach(), y.detach(), grad_F, op.t0, op.T, need_y, need_t)
         return gt, gy, None
 
 
@@ -68,8 +61,8 @@ class BatchedAdjointNFFT:
         F = op(t, y)                                      # t (B, N) float64, y (B, N); F (B, nf)
 
     The forward runs all series in one batched execution (one launch per
-    stage for the whole batch); the backward runs the hand-written VJP of each
-    series.
+    stage for the whole batch); so does the backward (the hand-written VJP,
+    cuna2_adjoint_backward_batch).
     """
 
     def __init__(self, B, N, nf, R=2, m=8, t0=None, T=None, dtype=torch.float32, device=None, graph=False):

@@ -65,9 +65,15 @@ struct cuna2_plan_st {
     const void *t, *y, *F;
     int64_t n;
     double t0, T;
+    int nbs;        // bootstrap resamples (0: not a bootstrap call)
+    unsigned seed;  // bootstrap seed the instantiated graph draws with
+    int nchan;      // value channels of a multi-channel call (0: none)
     cudaGraphExec_t exec;
+    cudaGraph_t graph;           // kept for the node handle below
+    cudaGraphNode_t seed_node;   // bootstrap: the draw kernel, whose seed a replay may update
   };
   std::vector<GraphEntry> graphs;
+  int64_t prof_n = -1;  // largest n cuna2_plan_profile has run eagerly
 };
 
 namespace cuna {
@@ -93,7 +99,10 @@ template <typename T> AccParams<T> make_params(const cuna2_plan_st *p) {
 
 int plan_workspace(cuna2_plan_st *p, size_t bytes, void **ws) {
   if (p->ws_bytes < bytes) {
-    for (auto &g : p->graphs) cudaGraphExecDestroy(g.exec);  // they point at the old workspace
+    for (auto &g : p->graphs) {  // they point at the old workspace
+      cudaGraphExecDestroy(g.exec);
+      if (g.graph) cudaGraphDestroy(g.graph);
+    }
     p->graphs.clear();
     if (p->ws) {
       CUNA_CK(cudaDeviceSynchronize());
@@ -114,6 +123,9 @@ int plan_workspace(cuna2_plan_st *p, size_t bytes, void **ws) {
 }
 
 // Optional per-launch event marks (cuna2_plan_profile).
+// The marks are recorded into a stream capture as event-record nodes
+// (cudaEventRecordExternal), so that replaying the graph timestamps each
+// launch's end on the device, with no host enqueue gaps in between.
 struct Prof {
   cudaEvent_t ev[16];
   const char *name[16];
@@ -122,7 +134,7 @@ struct Prof {
 inline void mark(Prof *pr, const char *name, cudaStream_t st) {
   if (pr && pr->n < 16) {
     pr->name[pr->n] = name;
-    cudaEventRecord(pr->ev[pr->n++], st);
+    cudaEventRecordWithFlags(pr->ev[pr->n++], st, cudaEventRecordExternal);
   }
 }
 
@@ -201,10 +213,18 @@ struct BinOut {
   int64_t *nrecords;
 };
 
+// cuna2_plan_time_grid: the gridding launch repeats `reps` times between two
+// events on the plan's stream (it is idempotent on the binned records).
+struct GridRepeat {
+  int reps;
+  cudaEvent_t e0, e1;
+};
+
 template <typename T>
 int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>::type *F, int64_t n,
                 double t0, double T_, cudaStream_t st, Prof *pr = nullptr, int nbs = 0, unsigned seed = 0,
-                const T *multi = nullptr, int nmulti = 0, const BinOut *bo = nullptr) {
+                const T *multi = nullptr, int nmulti = 0, const BinOut *bo = nullptr,
+                const GridRepeat *grep = nullptr) {
   typedef typename CxOf<T>::type C;
   typedef typename RecOf<T>::type Rec;
   if (n < 0 || (n > 0 && (!t || !y)) || (!F && !bo) || !(T_ > 0) || !std::isfinite(T_) || !std::isfinite(t0))
@@ -381,43 +401,54 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   else smg = grid_scatter_smem_bytes<T>(p->logTL);
   smg = (smg + 15) & ~(size_t)15;
   const dim3 gb(kGridThreads);
-  if (seg) {
-    const size_t sm = smg + segb;
-    if (p->grid_method == CUNA2_GRID_GATHER) {
-      if (cw8)
-        k_grid_acc_seg<T, 8><<<ggrid, gb, sm, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n, nslab, group, p->ng);
-      else
-        k_grid_acc_seg<T, 4><<<ggrid, gb, sm, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n, nslab, group, p->ng);
-    } else if (p->grid_method == CUNA2_GRID_FIXED) {
-      k_grid_fixed_seg<T, 4><<<ggrid, gb, sm, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n, nslab, group, p->ng);
+  auto launch_grid = [&]() -> int {
+    if (seg) {
+      const size_t sm = smg + segb;
+      if (p->grid_method == CUNA2_GRID_GATHER) {
+        if (cw8)
+          k_grid_acc_seg<T, 8><<<ggrid, gb, sm, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n, nslab, group, p->ng);
+        else
+          k_grid_acc_seg<T, 4><<<ggrid, gb, sm, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n, nslab, group, p->ng);
+      } else if (p->grid_method == CUNA2_GRID_FIXED) {
+        k_grid_fixed_seg<T, 4><<<ggrid, gb, sm, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n, nslab, group, p->ng);
+      } else {
+        k_grid_scatter_seg<T, 4><<<ggrid, gb, sm, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n, nslab, group,
+                                                       p->ng);
+      }
     } else {
-      k_grid_scatter_seg<T, 4><<<ggrid, gb, sm, st>>>(recs, loc, nch, ch2, (int)smg, grid, e, wts, n, nslab, group,
-                                                     p->ng);
+      const Rec *rc = recs;
+      const int *oc = offsets;
+      const T *wc = wts;
+      const int64_t nv = n, sstr = p->ng;
+      cudaError_t le;
+      const bool free_ = tail_free_gather(sizeof(T) == 4, p->m, p->tau) && !masked_gather_forced();
+      if (p->grid_method == CUNA2_GRID_GATHER && cw8 && wts && group >= 2) {
+        const size_t sm4 = grid_smem_bytes<T>(p->logTL, p->m, 4);
+        if (free_) le = launch_pdl(k_grid_acc_sg4<T, false>, ggrid, gb, sm4, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+        else le = launch_pdl(k_grid_acc_sg4<T>, ggrid, gb, sm4, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+      } else if (p->grid_method == CUNA2_GRID_GATHER) {
+        if (cw8 && free_)
+          le = launch_pdl(k_grid_acc<T, 8, false>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+        else if (cw8) le = launch_pdl(k_grid_acc<T, 8>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+        else if (free_)
+          le = launch_pdl(k_grid_acc<T, 4, false>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+        else le = launch_pdl(k_grid_acc<T, 4>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+      } else if (p->grid_method == CUNA2_GRID_FIXED) {
+        le = launch_pdl(k_grid_fixed<T>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+      } else {
+        le = launch_pdl(k_grid_scatter<T>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
+      }
+      CUNA_CK(le);
     }
+    CUNA_CK(cudaGetLastError());
+    return CUNA2_SUCCESS;
+  };
+  if (grep) {
+    CUNA_CK(cudaEventRecord(grep->e0, st));
+    for (int i = 0; i < grep->reps; ++i) CUNA_TRY(launch_grid());
+    CUNA_CK(cudaEventRecord(grep->e1, st));
   } else {
-    const Rec *rc = recs;
-    const int *oc = offsets;
-    const T *wc = wts;
-    const int64_t nv = n, sstr = p->ng;
-    cudaError_t le;
-    const bool free_ = tail_free_gather(sizeof(T) == 4, p->m, p->tau) && !masked_gather_forced();
-    if (p->grid_method == CUNA2_GRID_GATHER && cw8 && wts && group >= 2) {
-      const size_t sm4 = grid_smem_bytes<T>(p->logTL, p->m, 4);
-      if (free_) le = launch_pdl(k_grid_acc_sg4<T, false>, ggrid, gb, sm4, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
-      else le = launch_pdl(k_grid_acc_sg4<T>, ggrid, gb, sm4, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
-    } else if (p->grid_method == CUNA2_GRID_GATHER) {
-      if (cw8 && free_)
-        le = launch_pdl(k_grid_acc<T, 8, false>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
-      else if (cw8) le = launch_pdl(k_grid_acc<T, 8>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
-      else if (free_)
-        le = launch_pdl(k_grid_acc<T, 4, false>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
-      else le = launch_pdl(k_grid_acc<T, 4>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
-    } else if (p->grid_method == CUNA2_GRID_FIXED) {
-      le = launch_pdl(k_grid_fixed<T>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
-    } else {
-      le = launch_pdl(k_grid_scatter<T>, ggrid, gb, smg, st, rc, oc, grid, e, wc, nv, nslab, group, sstr);
-    }
-    CUNA_CK(le);
+    CUNA_TRY(launch_grid());
   }
   CUNA_CK(cudaGetLastError());
   mark(pr, "grid", st);
@@ -502,7 +533,10 @@ extern "C" int cuna2_plan_create(cuna2_plan *plan, int dtype, int64_t nf, int R,
 extern "C" int cuna2_plan_destroy(cuna2_plan p) {
   clear_error();
   if (!p) return CUNA2_SUCCESS;
-  for (auto &g : p->graphs) cudaGraphExecDestroy(g.exec);
+  for (auto &g : p->graphs) {
+      cudaGraphExecDestroy(g.exec);
+      if (g.graph) cudaGraphDestroy(g.graph);
+    }
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   if (p->ws) cudaFree(p->ws);
   if (p->bws) cudaFree(p->bws);
@@ -522,7 +556,7 @@ extern "C" int cuna2_plan_info(cuna2_plan p, int64_t *ng, double *tau) {
 namespace cuna {
 namespace {
 int run_graph(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0, double T,
-              cudaStream_t st);
+              cudaStream_t st, int nbs = 0, unsigned seed = 0, int nchan = 0);
 }
 }  // namespace cuna
 
@@ -539,41 +573,89 @@ extern "C" int cuna2_adjoint(cuna2_plan p, const double *t, const void *y, void 
 
 namespace cuna {
 namespace {
+// One transform of any kind: plain, bootstrap (nbs > 0) or multi-channel
+// (nchan > 0, y holding the channels).
 int run_any(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0, double T,
-            cudaStream_t st, Prof *pr) {
-  if (p->dtype == CUNA2_F32) return adjoint_run<float>(p, t, (const float *)y, (float2 *)F, n, t0, T, st, pr);
-  return adjoint_run<double>(p, t, (const double *)y, (double2 *)F, n, t0, T, st, pr);
+            cudaStream_t st, Prof *pr, int nbs = 0, unsigned seed = 0, int nchan = 0) {
+  if (p->dtype == CUNA2_F32)
+    return adjoint_run<float>(p, t, (const float *)y, (float2 *)F, n, t0, T, st, pr, nbs, seed,
+                              nchan ? (const float *)y : nullptr, nchan);
+  return adjoint_run<double>(p, t, (const double *)y, (double2 *)F, n, t0, T, st, pr, nbs, seed,
+                             nchan ? (const double *)y : nullptr, nchan);
+}
+
+// The kernel node of a captured bootstrap graph that draws the resamples
+// (k_boot_weights), or nullptr; its seed argument can be changed in the
+// instantiated graph.
+cudaGraphNode_t boot_seed_node(cuna2_plan p, cudaGraph_t graph) {
+  size_t nn = 0;
+  if (cudaGraphGetNodes(graph, nullptr, &nn) != cudaSuccess || nn == 0) return nullptr;
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (cudaGraphGetNodes(graph, nodes.data(), &nn) != cudaSuccess) return nullptr;
+  const void *fn = p->dtype == CUNA2_F32 ? (const void *)k_boot_weights<float> : (const void *)k_boot_weights<double>;
+  for (auto nd : nodes) {
+    cudaGraphNodeType ty;
+    if (cudaGraphNodeGetType(nd, &ty) != cudaSuccess || ty != cudaGraphNodeTypeKernel) continue;
+    cudaKernelNodeParams kp;
+    if (cudaGraphKernelNodeGetParams(nd, &kp) == cudaSuccess && kp.func == fn) return nd;
+  }
+  cudaGetLastError();
+  return nullptr;
+}
+
+// k_boot_weights(y, n, seed, wts): set the seed argument of its node in `exec`
+int set_boot_seed(cudaGraphExec_t exec, cudaGraphNode_t node, unsigned seed) {
+  cudaKernelNodeParams kp;
+  CUNA_CK(cudaGraphKernelNodeGetParams(node, &kp));
+  void *args[4] = {kp.kernelParams[0], kp.kernelParams[1], &seed, kp.kernelParams[3]};
+  kp.kernelParams = args;
+  kp.extra = nullptr;
+  CUNA_CK(cudaGraphExecKernelNodeSetParams(exec, node, &kp));
+  return CUNA2_SUCCESS;
 }
 
 // Graph path: capture the launch sequence once per argument set on a private
 // stream, then replay it on the caller's stream.
 int run_graph(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0, double T,
-              cudaStream_t st) {
+              cudaStream_t st, int nbs, unsigned seed, int nchan) {
   for (auto &g : p->graphs)
-    if (g.t == t && g.y == y && g.F == F && g.n == n && g.t0 == t0 && g.T == T) {
+    if (g.t == t && g.y == y && g.F == F && g.n == n && g.t0 == t0 && g.T == T && g.nbs == nbs &&
+        g.nchan == nchan && (g.seed == seed || g.seed_node)) {
+      if (g.seed != seed) {  // same resampling, new draws: update the draw kernel's seed argument
+        CUNA_TRY(set_boot_seed(g.exec, g.seed_node, seed));
+        g.seed = seed;
+      }
       CUNA_CK(cudaGraphLaunch(g.exec, st));
       return CUNA2_SUCCESS;
     }
   // run once eagerly: sizes the workspace (allocation is not capturable) and
   // produces this call's result
-  CUNA_TRY(run_any(p, t, y, F, n, t0, T, st, nullptr));
+  CUNA_TRY(run_any(p, t, y, F, n, t0, T, st, nullptr, nbs, seed, nchan));
   if (!p->cap_stream) CUNA_CK(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking));
   CUNA_CK(cudaStreamSynchronize(st));
   CUNA_CK(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
-  int s = run_any(p, t, y, F, n, t0, T, p->cap_stream, nullptr);
+  int s = run_any(p, t, y, F, n, t0, T, p->cap_stream, nullptr, nbs, seed, nchan);
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamEndCapture(p->cap_stream, &graph);
   if (s) return s;
   if (e != cudaSuccess) return fail_cuda(e, "cudaStreamEndCapture");
   cudaGraphExec_t exec = nullptr;
   e = cudaGraphInstantiate(&exec, graph, 0);
-  cudaGraphDestroy(graph);
-  if (e != cudaSuccess) return fail_cuda(e, "cudaGraphInstantiate");
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return fail_cuda(e, "cudaGraphInstantiate");
+  }
+  cudaGraphNode_t seed_node = nbs > 0 ? boot_seed_node(p, graph) : nullptr;
+  if (!seed_node) {  // nothing to update later: the graph itself is not needed
+    cudaGraphDestroy(graph);
+    graph = nullptr;
+  }
   if (p->graphs.size() >= 64) {
     cudaGraphExecDestroy(p->graphs.front().exec);
+    if (p->graphs.front().graph) cudaGraphDestroy(p->graphs.front().graph);
     p->graphs.erase(p->graphs.begin());
   }
-  p->graphs.push_back({t, y, F, n, t0, T, exec});
+  p->graphs.push_back({t, y, F, n, t0, T, nbs, seed, nchan, exec, graph, seed_node});
   return CUNA2_SUCCESS;
 }
 }  // namespace
@@ -648,20 +730,64 @@ extern "C" int cuna2_plan_profile(cuna2_plan p, const double *t, const void *y, 
   clear_error();
   if (!p || !stage_ms || !nstages) return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
   std::lock_guard<std::mutex> lk(p->mu);
+  *nstages = 0;
+  // the first profile of a plan (or one with more samples) runs once eagerly:
+  // that sizes the workspace (allocation is not capturable) and does the
+  // one-time kernel set-up; later profiles replay inputs untouched since the
+  // caller last evicted them
+  if (n > p->prof_n) {
+    CUNA_TRY(run_any(p, t, y, F, n, t0, T, st, nullptr));
+    p->prof_n = n;
+  }
+  if (!p->cap_stream) CUNA_CK(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking));
+  CUNA_CK(cudaStreamSynchronize(st));
   Prof pr;
   for (int i = 0; i < 16; ++i) CUNA_CK(cudaEventCreate(&pr.ev[i]));
-  int s = run_any(p, t, y, F, n, t0, T, st, &pr);
-  if (!s) {
-    cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) s = fail_cuda(e, "cudaStreamSynchronize");
+  // the launch sequence with an event after each launch, captured as one
+  // graph; launches are serialised (no dependent launch) so that each
+  // interval is one kernel
+  pdl_suppress(true);
+  cudaEvent_t gap0 = nullptr, gap1 = nullptr;  // two event nodes with nothing between: the gap each mark adds
+  CUNA_CK(cudaEventCreate(&gap0));
+  CUNA_CK(cudaEventCreate(&gap1));
+  cudaError_t e = cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaEventRecordWithFlags(gap0, p->cap_stream, cudaEventRecordExternal);
+    cudaEventRecordWithFlags(gap1, p->cap_stream, cudaEventRecordExternal);
   }
+  int s = e == cudaSuccess ? run_any(p, t, y, F, n, t0, T, p->cap_stream, &pr) : fail_cuda(e, "begin capture");
+  cudaGraph_t graph = nullptr;
+  if (e == cudaSuccess) {
+    const cudaError_t e2 = cudaStreamEndCapture(p->cap_stream, &graph);
+    if (!s && e2 != cudaSuccess) s = fail_cuda(e2, "cudaStreamEndCapture");
+  }
+  pdl_suppress(false);
+  cudaGraphExec_t exec = nullptr;
+  if (!s) {
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) s = fail_cuda(e, "cudaGraphInstantiate");
+  }
+  if (graph) cudaGraphDestroy(graph);
+  if (!s) {
+    e = cudaGraphLaunch(exec, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) s = fail_cuda(e, "profile graph launch");
+  }
+  if (exec) cudaGraphExecDestroy(exec);
   int k = 0;
   for (int i = 1; !s && i < pr.n && k < max_stages; ++i, ++k) {
     cudaEventElapsedTime(&stage_ms[k], pr.ev[i - 1], pr.ev[i]);
     if (stage_names) stage_names[k] = pr.name[i];
   }
+  if (!s && k < max_stages) {
+    cudaEventElapsedTime(&stage_ms[k], gap0, gap1);
+    if (stage_names) stage_names[k] = "event_gap";
+    ++k;
+  }
   *nstages = k;
   for (int i = 0; i < 16; ++i) cudaEventDestroy(pr.ev[i]);
+  cudaEventDestroy(gap0);
+  cudaEventDestroy(gap1);
   return s;
 }
 
@@ -675,7 +801,11 @@ bool schedule_ok(const cuna2_plan_st *p, int log_tile, int method) {
   return log_tile == logng || (1 << log_tile) >= 2 * p->m;
 }
 void drop_graphs(cuna2_plan_st *p) {
-  for (auto &g : p->graphs) cudaGraphExecDestroy(g.exec);
+  p->prof_n = -1;  // a new schedule may need a larger workspace
+  for (auto &g : p->graphs) {
+      cudaGraphExecDestroy(g.exec);
+      if (g.graph) cudaGraphDestroy(g.graph);
+    }
   p->graphs.clear();
 }
 }  // namespace
@@ -869,6 +999,7 @@ extern "C" int cuna2_adjoint_bootstrap(cuna2_plan p, const double *t, const void
   if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
   if (nbs < 1) return fail(CUNA2_ERROR_INVALID_VALUE, "nbs must be >= 1");
   std::lock_guard<std::mutex> lk(p->mu);
+  if (p->use_graph) return run_graph(p, t, y, F, n, t0, T, st, nbs, seed, 0);
   if (p->dtype == CUNA2_F32)
     return adjoint_run<float>(p, t, (const float *)y, (float2 *)F, n, t0, T, st, nullptr, nbs, seed);
   return adjoint_run<double>(p, t, (const double *)y, (double2 *)F, n, t0, T, st, nullptr, nbs, seed);
@@ -876,14 +1007,22 @@ extern "C" int cuna2_adjoint_bootstrap(cuna2_plan p, const double *t, const void
 
 namespace cuna {
 namespace {
+// Vector-Jacobian products of nser series of n samples each on one plan:
+// series s has t + s*n, y + s*n, G + s*nf, gy + s*n, gt + s*n and its own
+// t0s[s], Ts[s].  Series go in groups of up to kBwdSeries, one launch per
+// stage per group; the plan's backward workspace holds two packed complex
+// grids per series of a group.
 template <typename T>
 int backward_run(cuna2_plan_st *p, const double *t, const T *y, const typename CxOf<T>::type *G, T *gy, double *gt,
-                 int64_t n, double t0, double T_, cudaStream_t st) {
+                 int64_t n, int nser, const double *t0s, const double *Ts, cudaStream_t st) {
   typedef typename CxOf<T>::type C;
-  if (n < 0 || (n > 0 && (!t || (gt && !y))) || !G || !(T_ > 0) || !std::isfinite(T_) || !std::isfinite(t0))
-    return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument (n=%lld T=%g)", (long long)n, T_);
+  if (n < 0 || nser < 1 || !t0s || !Ts || (n > 0 && (!t || (gt && !y))) || !G)
+    return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument (n=%lld nseries=%d)", (long long)n, nser);
+  for (int s = 0; s < nser; ++s)
+    if (!(Ts[s] > 0) || !std::isfinite(Ts[s]) || !std::isfinite(t0s[s]))
+      return fail(CUNA2_ERROR_INVALID_VALUE, "series %d: T = %g, t0 = %g", s, Ts[s], t0s[s]);
+  if (n > ((int64_t)1 << 30)) return fail(CUNA2_ERROR_UNSUPPORTED, "n > 2^30 samples per series");
   if (n == 0 || (!gy && !gt)) return CUNA2_SUCCESS;
-  const PhaseMul pm = phase_setup(t0, T_);
   const AccParams<T> e = make_params<T>(p);
   const FftDev<T> f = to_dev<T>(p->geom);
   BwdSpec<T> sp;
@@ -893,51 +1032,70 @@ int backward_run(cuna2_plan_st *p, const double *t, const T *y, const typename C
   sp.c0b = (T)(1.0 / sqrt(4.0 * kPi * p->tau));
   sp.c1 = (T)(4.0 * kPi * kPi * p->tau / ((double)p->ng * (double)p->ng));
   sp.twk = (T)(2.0 / (double)p->ng);
-  const double tscale = (double)p->ng / T_;
   const int L = 1 << p->geom.logL;
-  if (p->small) {
-    static char attr;
-    if (!setup_done(&attr)) {
-      CUNA_CK(cudaFuncSetAttribute(k_bwd_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-      mark_setup_done(&attr);
+  const int group = std::min(nser, kBwdSeries);
+  BwdSeries *ser = new BwdSeries();  // 8 KB of launch parameters, filled per group
+  struct Del {
+    BwdSeries *q;
+    ~Del() { delete q; }
+  } del{ser};
+  C *z = nullptr, *r = nullptr;
+  if (!p->small) {
+    const size_t need = 2 * sizeof(C) * (size_t)L * group;
+    if (p->bws_bytes < need) {
+      if (p->bws) {
+        CUNA_CK(cudaDeviceSynchronize());
+        CUNA_CK(cudaFree(p->bws));
+        p->bws = nullptr;
+        p->bws_bytes = 0;
+      }
+      cudaError_t er = cudaMalloc(&p->bws, need);
+      if (er != cudaSuccess) return fail(CUNA2_ERROR_ALLOC, "backward workspace: %s", cudaGetErrorString(er));
+      p->bws_bytes = need;
     }
-    const size_t smem = sizeof(C) * (size_t)fft_pitch(L, 1);
-    const int threads = std::max(32, std::min(sizeof(T) == 4 ? 1024 : 512, L / kFftE));
-    k_bwd_small<T><<<1, std::max(threads, 32), smem, st>>>(t, y, n, pm, e, sp, f, gy, gt, tscale);
-    CUNA_CK(cudaGetLastError());
-    return CUNA2_SUCCESS;
+    z = (C *)p->bws;
+    r = z + (size_t)L * group;
   }
-  const size_t need = 2 * sizeof(C) * (size_t)L;
-  if (p->bws_bytes < need) {
-    if (p->bws) {
-      CUNA_CK(cudaDeviceSynchronize());
-      CUNA_CK(cudaFree(p->bws));
-      p->bws = nullptr;
-      p->bws_bytes = 0;
-    }
-    cudaError_t er = cudaMalloc(&p->bws, need);
-    if (er != cudaSuccess) return fail(CUNA2_ERROR_ALLOC, "backward workspace: %s", cudaGetErrorString(er));
-    p->bws_bytes = need;
-  }
-  C *z = (C *)p->bws, *r = z + L;
-  const int elems = sizeof(T) == 4 ? kPassElemsF32 : kPassElemsF64;
-  const int threads = elems / kFftE;
-  const int L1 = 1 << p->geom.logL1, L2 = 1 << p->geom.logL2;
-  const int BA = elems / L1, BB = elems / L2;
-  const size_t smemA = sizeof(C) * (size_t)BA * fft_pitch(L1, BA);
-  const size_t smemB = sizeof(C) * (size_t)BB * fft_pitch(L2, BB);
-  static char attr2;
-  if (!setup_done(&attr2)) {
+  static char attr;
+  if (!setup_done(&attr)) {
+    CUNA_CK(cudaFuncSetAttribute(k_bwd_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     CUNA_CK(cudaFuncSetAttribute(k_bwd_colpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CUNA_CK(cudaFuncSetAttribute(k_bwd_rowpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    mark_setup_done(&attr2);
+    mark_setup_done(&attr);
   }
-  k_bwd_colpass<T><<<L2 / BA, threads, smemA, st>>>(sp, z, f);
-  CUNA_CK(cudaGetLastError());
-  k_bwd_rowpass<T><<<L1 / BB, threads, smemB, st>>>(z, r, f);
-  CUNA_CK(cudaGetLastError());
-  k_bwd_interp<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(t, y, n, pm, e, (const T *)r, gy, gt, tscale);
-  CUNA_CK(cudaGetLastError());
+  for (int s0 = 0; s0 < nser; s0 += group) {
+    const int ns = std::min(group, nser - s0);
+    for (int s = 0; s < ns; ++s) {
+      ser->pm[s] = phase_setup(t0s[s0 + s], Ts[s0 + s]);
+      ser->tscale[s] = (double)p->ng / Ts[s0 + s];
+    }
+    const double *tg = t + (int64_t)s0 * n;
+    const T *yg = y ? y + (int64_t)s0 * n : nullptr;
+    T *gyg = gy ? gy + (int64_t)s0 * n : nullptr;
+    double *gtg = gt ? gt + (int64_t)s0 * n : nullptr;
+    BwdSpec<T> spg = sp;
+    spg.G = G + (int64_t)s0 * p->nf;
+    if (p->small) {
+      const size_t smem = sizeof(C) * (size_t)fft_pitch(L, 1);
+      const int threads = std::max(32, std::min(sizeof(T) == 4 ? 1024 : 512, L / kFftE));
+      k_bwd_small<T><<<ns, threads, smem, st>>>(tg, yg, n, *ser, e, spg, f, gyg, gtg);
+      CUNA_CK(cudaGetLastError());
+      continue;
+    }
+    const int elems = sizeof(T) == 4 ? kPassElemsF32 : kPassElemsF64;
+    const int threads = elems / kFftE;
+    const int L1 = 1 << p->geom.logL1, L2 = 1 << p->geom.logL2;
+    const int BA = elems / L1, BB = elems / L2;
+    const size_t smemA = sizeof(C) * (size_t)BA * fft_pitch(L1, BA);
+    const size_t smemB = sizeof(C) * (size_t)BB * fft_pitch(L2, BB);
+    k_bwd_colpass<T><<<dim3(L2 / BA, ns), threads, smemA, st>>>(spg, z, f);
+    CUNA_CK(cudaGetLastError());
+    k_bwd_rowpass<T><<<dim3(L1 / BB, ns), threads, smemB, st>>>(z, r, f);
+    CUNA_CK(cudaGetLastError());
+    const int64_t tot = n * ns;
+    k_bwd_interp<T><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(tg, yg, n, ns, *ser, e, (const T *)r, gyg, gtg);
+    CUNA_CK(cudaGetLastError());
+  }
   return CUNA2_SUCCESS;
 }
 }  // namespace
@@ -949,8 +1107,22 @@ extern "C" int cuna2_adjoint_backward(cuna2_plan p, const double *t, const void 
   if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
   std::lock_guard<std::mutex> lk(p->mu);
   if (p->dtype == CUNA2_F32)
-    return backward_run<float>(p, t, (const float *)y, (const float2 *)G, (float *)grad_y, grad_t, n, t0, T, st);
-  return backward_run<double>(p, t, (const double *)y, (const double2 *)G, (double *)grad_y, grad_t, n, t0, T, st);
+    return backward_run<float>(p, t, (const float *)y, (const float2 *)G, (float *)grad_y, grad_t, n, 1, &t0, &T, st);
+  return backward_run<double>(p, t, (const double *)y, (const double2 *)G, (double *)grad_y, grad_t, n, 1, &t0, &T,
+                              st);
+}
+
+extern "C" int cuna2_adjoint_backward_batch(cuna2_plan p, const double *t, const void *y, const void *G,
+                                            void *grad_y, double *grad_t, int64_t n, int nseries, const double *t0,
+                                            const double *T, cudaStream_t st) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (p->dtype == CUNA2_F32)
+    return backward_run<float>(p, t, (const float *)y, (const float2 *)G, (float *)grad_y, grad_t, n, nseries, t0, T,
+                               st);
+  return backward_run<double>(p, t, (const double *)y, (const double2 *)G, (double *)grad_y, grad_t, n, nseries, t0,
+                              T, st);
 }
 
 extern "C" int cuna2_adjoint_multi(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, int nchan,
@@ -959,6 +1131,7 @@ extern "C" int cuna2_adjoint_multi(cuna2_plan p, const double *t, const void *y,
   if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
   if (!y || nchan < 1) return fail(CUNA2_ERROR_INVALID_VALUE, "need nchan >= 1 value channels");
   std::lock_guard<std::mutex> lk(p->mu);
+  if (p->use_graph) return run_graph(p, t, y, F, n, t0, T, st, 0, 0, nchan);
   if (p->dtype == CUNA2_F32)
     return adjoint_run<float>(p, t, (const float *)y, (float2 *)F, n, t0, T, st, nullptr, 0, 0, (const float *)y,
                               nchan);
@@ -1013,4 +1186,34 @@ extern "C" int cuna2_plan_inspect_bins(cuna2_plan p, const double *t, const void
   if (p->dtype == CUNA2_F32)
     return adjoint_run<float>(p, t, (const float *)y, nullptr, n, t0, T, st, nullptr, 0, 0, nullptr, 0, &bo);
   return adjoint_run<double>(p, t, (const double *)y, nullptr, n, t0, T, st, nullptr, 0, 0, nullptr, 0, &bo);
+}
+
+extern "C" int cuna2_plan_time_grid(cuna2_plan p, const double *t, const void *y, void *F, int64_t n, double t0,
+                                    double T, int reps, cudaStream_t st, float *ms_per_launch) {
+  clear_error();
+  if (!p || !ms_per_launch || reps < 1 || reps > 10000) return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (p->small) return fail(CUNA2_ERROR_UNSUPPORTED, "single-CTA plans have no separate gridding launch");
+  GridRepeat gr{reps, nullptr, nullptr};
+  CUNA_CK(cudaEventCreate(&gr.e0));
+  cudaError_t e = cudaEventCreate(&gr.e1);
+  if (e != cudaSuccess) {
+    cudaEventDestroy(gr.e0);
+    return fail_cuda(e, "cudaEventCreate");
+  }
+  int s = p->dtype == CUNA2_F32
+              ? adjoint_run<float>(p, t, (const float *)y, (float2 *)F, n, t0, T, st, nullptr, 0, 0, nullptr, 0,
+                                   nullptr, &gr)
+              : adjoint_run<double>(p, t, (const double *)y, (double2 *)F, n, t0, T, st, nullptr, 0, 0, nullptr, 0,
+                                    nullptr, &gr);
+  if (!s) {
+    e = cudaStreamSynchronize(st);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, gr.e0, gr.e1);
+    if (e != cudaSuccess) s = fail_cuda(e, "timing the gridding launches");
+    else *ms_per_launch = ms / (float)reps;
+  }
+  cudaEventDestroy(gr.e0);
+  cudaEventDestroy(gr.e1);
+  return s;
 }

@@ -1077,6 +1077,15 @@ template <typename T> struct BwdSpec {
   }
 };
 
+// Per-series constants of a batch of backward passes (up to kBwdSeries
+// series per launch, passed by value): the phase multiplier of x = (t - t0)/T
+// and ng / T, the chain-rule factor of dL/dt.
+constexpr int kBwdSeries = 256;
+struct BwdSeries {
+  PhaseMul pm[kBwdSeries];
+  double tscale[kBwdSeries];
+};
+
 // interpolation of R at one sample: accumulates both gradient sums
 template <typename T, class Rget>
 __device__ __forceinline__ void bwd_sample(const Rget &R, int cell, T fr, int m, int ng, T k1, T inv2tau,
@@ -1094,12 +1103,22 @@ __device__ __forceinline__ void bwd_sample(const Rget &R, int cell, T fr, int m,
   }
 }
 
-// Single CTA: spectrum -> shared memory -> FFT -> interpolation at every sample.
+// Single CTA per series: spectrum -> shared memory -> FFT -> interpolation at
+// every sample.  CTA b handles series b of the batch (samples b*n.., upstream
+// gradient b*nf..).
 template <typename T>
 __global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512) k_bwd_small(
-    const double *__restrict__ t, const T *__restrict__ y, int64_t n, PhaseMul pm, AccParams<T> e, BwdSpec<T> sp,
-    FftDev<T> f, T *__restrict__ gy, double *__restrict__ gt, double tscale) {
+    const double *__restrict__ t, const T *__restrict__ y, int64_t n, const __grid_constant__ BwdSeries ser,
+    AccParams<T> e, BwdSpec<T> sp, FftDev<T> f, T *__restrict__ gy, double *__restrict__ gt) {
   typedef typename CxOf<T>::type C;
+  const int b = blockIdx.x;
+  const PhaseMul pm = ser.pm[b];
+  const double tscale = ser.tscale[b];
+  t += (int64_t)b * n;
+  y += (int64_t)b * n;
+  if (gy) gy += (int64_t)b * n;
+  if (gt) gt += (int64_t)b * n;
+  sp.G += (int64_t)b * 2 * sp.K;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int L = 1 << f.logL;
   const int pitch = fft_pitch(L, 1);
@@ -1140,6 +1159,8 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_bwd_colpass(BwdS
   typedef typename CxOf<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *s = reinterpret_cast<C *>(smem_raw);
+  sp.G += (int64_t)blockIdx.y * 2 * sp.K;  // series blockIdx.y of a batch
+  z += (int64_t)blockIdx.y << f.logL;
   const int L2 = 1 << f.logL2;
   const int logB = ilog2i((int64_t)blockDim.x * kFftE) - f.logL1;
   const int B = 1 << logB;
@@ -1172,6 +1193,8 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_bwd_rowpass(cons
   typedef typename CxOf<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *s = reinterpret_cast<C *>(smem_raw);
+  z += (int64_t)blockIdx.y << f.logL;  // series blockIdx.y of a batch
+  r += (int64_t)blockIdx.y << f.logL;
   const int logB = ilog2i((int64_t)blockDim.x * kFftE) - f.logL2;
   const int B = 1 << logB;
   const int pitch = fft_pitch(1 << f.logL2, B);
@@ -1181,21 +1204,26 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_bwd_rowpass(cons
   fft_fused<T, true, false, true>(s, pitch, f.logL2, logB, f.tw2, src, dst);
 }
 
+// interpolation at samples j < n * nser of a batch: series s = j / n reads its
+// own real field R + s * ng and constants ser.*[s]
 template <typename T>
 __global__ void __launch_bounds__(256) k_bwd_interp(const double *__restrict__ t, const T *__restrict__ y, int64_t n,
-                                                    PhaseMul pm, AccParams<T> e, const T *__restrict__ R,
-                                                    T *__restrict__ gy, double *__restrict__ gt, double tscale) {
+                                                    int nser, const __grid_constant__ BwdSeries ser, AccParams<T> e,
+                                                    const T *__restrict__ R, T *__restrict__ gy,
+                                                    double *__restrict__ gt) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
+  if (j >= n * nser) return;
+  const int s = (int)(j / n);
   int cell;
   T fr;
-  reduce_sample<T>(t[j], pm, e.ng, cell, fr);
+  reduce_sample<T>(t[j], ser.pm[s], e.ng, cell, fr);
   const T inv2tau = (T)2.0 * e.e3c * (T)-1.0;
-  auto Rg = [&](int c) -> T { return __ldg(&R[c]); };
+  const T *Rs = R + (int64_t)s * e.ng;
+  auto Rg = [&](int c) -> T { return __ldg(&Rs[c]); };
   T a, b;
   bwd_sample<T>(Rg, cell, fr, e.m, (int)e.ng, e.k1, inv2tau, a, b);
   if (gy) gy[j] = a;
-  if (gt) gt[j] = tscale * (double)y[j] * (double)b;
+  if (gt) gt[j] = ser.tscale[s] * (double)y[j] * (double)b;
 }
 
 // ---------------------------------------------------------------------------

@@ -126,6 +126,21 @@ __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 2) k_bgrid(
                      1, 0);
 }
 
+// The same tiles in gather form (grid_tile_body): CW = 8 cells per thread on
+// 2048-cell tiles, else 4; MASKED as tail_free_gather decides.
+template <typename T, int CW, bool MASKED>
+__global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 4 : 2) k_bgrid_gather(
+    const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
+    const BDesc<T> *__restrict__ D, const int *__restrict__ tile_series) {
+  const int gt = blockIdx.x;
+  const BDesc<T> d = D[tile_series[gt]];
+  typedef const typename RecOf<T>::type *RecPtr;
+  const RecPtr rp = recs;
+  const T *no_wts = nullptr;
+  grid_tile_body<T, CW, RecPtr, 1, MASKED>(rp, off[gt], off[gt + 1], (gt - d.tile0) << d.e.logTL, grid + d.g_off,
+                                           d.e, no_wts, (int64_t)0, 0, 1, (int64_t)0);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_bcolpass(T *grid, const BDesc<T> *__restrict__ D,
                                                                          const Item *__restrict__ items) {
@@ -259,6 +274,9 @@ template <typename V> int upload(const std::vector<V> &h, void **d) {
 struct cuna2_batch_plan_st {
   int dtype, R, m, nseries;
   double tau;
+  // gridding schedule of the large series (cuna2_batch_set_schedule)
+  int log_tile = 12;
+  int grid_method = CUNA2_GRID_FIXED;
   int64_t n_total = 0, f_total = 0;
   std::vector<int64_t> n, nf;
   std::vector<double> t0, T;
@@ -319,7 +337,7 @@ template <typename T> int batch_build(cuna2_batch_plan_st *p) {
     const int64_t nf = p->nf[s], ng = nf * p->R, L = ng / 2;
     const int logL = ilog2i(L);
     const bool is_small = logL <= single_log;
-    const int logTL = ng <= 8192 ? ilog2i(ng) : 12;
+    const int logTL = std::min(ilog2i(ng), p->log_tile);
     BDesc<T> &d = desc[s];
     d.e = series_params<T>(nf, p->R, p->m, p->tau, logTL);
     d.pm = phase_setup(p->t0[s], p->T[s]);
@@ -431,6 +449,10 @@ int batch_run(cuna2_batch_plan_st *p, const double *t, const T *y, typename CxOf
   if (!setup_done(&attr)) {
     CUNA_CK(cudaFuncSetAttribute(k_bsmall<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
     CUNA_CK(cudaFuncSetAttribute(k_bgrid<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CUNA_CK(cudaFuncSetAttribute(k_bgrid_gather<T, 8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CUNA_CK(cudaFuncSetAttribute(k_bgrid_gather<T, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CUNA_CK(cudaFuncSetAttribute(k_bgrid_gather<T, 4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CUNA_CK(cudaFuncSetAttribute(k_bgrid_gather<T, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CUNA_CK(cudaFuncSetAttribute(k_bcolpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CUNA_CK(cudaFuncSetAttribute(k_browpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     mark_setup_done(&attr);
@@ -472,9 +494,22 @@ int batch_run(cuna2_batch_plan_st *p, const double *t, const T *y, typename CxOf
                                                                p->resv, (Rec *)p->recs);
       CUNA_CK(cudaGetLastError());
     }
-    const size_t smg = grid_fixed_smem_bytes<T>(12, p->m);
-    k_bgrid<T><<<ntl, kGridThreads, smg, st>>>((const Rec *)p->recs, p->offsets, (T *)p->grid, D,
-                                               (const int *)p->d_tile_series);
+    const Rec *rc = (const Rec *)p->recs;
+    const int *ts = (const int *)p->d_tile_series;
+    if (p->grid_method == CUNA2_GRID_GATHER) {
+      const size_t smg = (grid_smem_bytes<T>(p->log_tile, p->m) + 15) & ~(size_t)15;
+      const bool free_ = tail_free_gather(sizeof(T) == 4, p->m, p->tau) && !masked_gather_forced();
+      if (p->log_tile == 11) {
+        if (free_) k_bgrid_gather<T, 8, false><<<ntl, kGridThreads, smg, st>>>(rc, p->offsets, (T *)p->grid, D, ts);
+        else k_bgrid_gather<T, 8, true><<<ntl, kGridThreads, smg, st>>>(rc, p->offsets, (T *)p->grid, D, ts);
+      } else {
+        if (free_) k_bgrid_gather<T, 4, false><<<ntl, kGridThreads, smg, st>>>(rc, p->offsets, (T *)p->grid, D, ts);
+        else k_bgrid_gather<T, 4, true><<<ntl, kGridThreads, smg, st>>>(rc, p->offsets, (T *)p->grid, D, ts);
+      }
+    } else {
+      const size_t smg = grid_fixed_smem_bytes<T>(p->log_tile, p->m);
+      k_bgrid<T><<<ntl, kGridThreads, smg, st>>>(rc, p->offsets, (T *)p->grid, D, ts);
+    }
     CUNA_CK(cudaGetLastError());
     if (p->fft_ct) {  // one column and one row launch per size class
       for (size_t c = 0; c < p->fft_classes.size(); ++c) {
@@ -527,18 +562,46 @@ int batch_graph(cuna2_batch_plan_st *p, const double *t, const void *y, void *F,
   return CUNA2_SUCCESS;
 }
 
-void batch_free(cuna2_batch_plan_st *p) {
+// Everything batch_build makes (tables, workspace, streams, graphs), so that
+// it can build the plan again under another schedule.
+void batch_release(cuna2_batch_plan_st *p) {
   for (auto &g : p->graphs) cudaGraphExecDestroy(g.exec);
+  p->graphs.clear();
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   if (p->side) cudaStreamDestroy(p->side);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_join) cudaEventDestroy(p->ev_join);
-  for (void *d : {p->d_desc, p->d_count_items, p->d_tile_series, p->d_col_items, p->d_row_items, p->d_small_list,
-                  p->d_fft_list,
-                  p->ws})
-    if (d) cudaFree(d);
+  p->cap_stream = p->side = nullptr;
+  p->ev_fork = p->ev_join = nullptr;
+  for (void **d : {&p->d_desc, &p->d_count_items, &p->d_tile_series, &p->d_col_items, &p->d_row_items,
+                   &p->d_small_list, &p->d_fft_list, &p->ws}) {
+    if (*d) cudaFree(*d);
+    *d = nullptr;
+  }
   free(p->host_desc);
+  p->host_desc = nullptr;
+  p->desc_bytes = 0;
+  p->tiles_total = 0;
+  p->large_samples = p->grid_total = 0;
+  p->n_count_items = p->n_col_items = p->n_row_items = 0;
+  p->smem_col = p->smem_row = p->smem_bin = 0;
+  p->max_large_tiles = 0;
+  p->small_classes.clear();
+  p->small_class_off.clear();
+  p->fft_classes.clear();
+  p->fft_class_off.clear();
+  p->fft_ct = false;
+}
+
+void batch_free(cuna2_batch_plan_st *p) {
+  batch_release(p);
   delete p;
+}
+
+int batch_rebuild(cuna2_batch_plan_st *p) {
+  CUNA_CK(cudaDeviceSynchronize());  // nothing may still use the old tables
+  batch_release(p);
+  return p->dtype == CUNA2_F32 ? batch_build<float>(p) : batch_build<double>(p);
 }
 
 template <typename T> void set_times_host(cuna2_batch_plan_st *p) {
@@ -631,4 +694,101 @@ extern "C" int cuna2_batch_adjoint(cuna2_batch_plan p, const double *t, const vo
   if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
   std::lock_guard<std::mutex> lk(p->mu);
   return p->use_graph ? batch_graph(p, t, y, F, st) : batch_any(p, t, y, F, st);
+}
+
+extern "C" int cuna2_batch_set_schedule(cuna2_batch_plan p, int log_tile, int grid_method) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  if (grid_method != CUNA2_GRID_GATHER && grid_method != CUNA2_GRID_FIXED)
+    return fail(CUNA2_ERROR_INVALID_VALUE, "batched plans grid in gather or fixed-point form");
+  if (log_tile < 10 || log_tile > 12) return fail(CUNA2_ERROR_INVALID_VALUE, "log_tile must be 10, 11 or 12");
+  if (2 * p->m > (1 << log_tile)) return fail(CUNA2_ERROR_INVALID_VALUE, "tiles must span at least 2m cells");
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (p->log_tile == log_tile && p->grid_method == grid_method) return CUNA2_SUCCESS;
+  const int old_lt = p->log_tile, old_gm = p->grid_method;
+  p->log_tile = log_tile;
+  p->grid_method = grid_method;
+  const int s = batch_rebuild(p);
+  if (s) {  // put the previous schedule back
+    p->log_tile = old_lt;
+    p->grid_method = old_gm;
+    batch_rebuild(p);
+  }
+  return s;
+}
+
+extern "C" int cuna2_batch_get_schedule(cuna2_batch_plan p, int *log_tile, int *grid_method) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  if (log_tile) *log_tile = p->log_tile;
+  if (grid_method) *grid_method = p->grid_method;
+  return CUNA2_SUCCESS;
+}
+
+extern "C" int cuna2_batch_autotune(cuna2_batch_plan p, const double *t, const void *y, void *F, cudaStream_t st,
+                                    int reps, float *best_ms) {
+  clear_error();
+  if (!p || reps < 1) return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
+  bool graph;
+  {
+    std::lock_guard<std::mutex> lk(p->mu);
+    graph = p->use_graph;
+    p->use_graph = false;  // time eager executions; no graphs of trial schedules
+  }
+  // a buffer of twice the L2 size, overwritten before each timed run so the
+  // inputs come from HBM
+  int dev = 0, l2 = 0;
+  CUNA_CK(cudaGetDevice(&dev));
+  CUNA_CK(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+  void *flush = nullptr;
+  if (cudaMalloc(&flush, 2 * (size_t)l2) != cudaSuccess) {
+    cudaGetLastError();
+    flush = nullptr;
+  }
+  cudaEvent_t e0, e1;
+  CUNA_CK(cudaEventCreate(&e0));
+  CUNA_CK(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int best_lt = p->log_tile, best_gm = p->grid_method, status = CUNA2_SUCCESS;
+  for (int gm : {CUNA2_GRID_FIXED, CUNA2_GRID_GATHER}) {
+    for (int lt = 10; lt <= 12; ++lt) {
+      if (2 * p->m > (1 << lt)) continue;
+      if (cuna2_batch_set_schedule(p, lt, gm) != CUNA2_SUCCESS) continue;
+      float ms = 1e30f;
+      int s = cuna2_batch_adjoint(p, t, y, F, st);  // warm-up
+      for (int r = 0; !s && r < reps; ++r) {
+        if (flush) cudaMemsetAsync(flush, r & 0xff, 2 * (size_t)l2, st);
+        cudaEventRecord(e0, st);
+        s = cuna2_batch_adjoint(p, t, y, F, st);
+        cudaEventRecord(e1, st);
+        if (!s && cudaEventSynchronize(e1) == cudaSuccess) {
+          float x = 0.f;
+          cudaEventElapsedTime(&x, e0, e1);
+          ms = std::min(ms, x);
+        }
+      }
+      if (s) {
+        status = s;
+        break;
+      }
+      if (ms < best) {
+        best = ms;
+        best_lt = lt;
+        best_gm = gm;
+      }
+    }
+    if (status) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (flush) cudaFree(flush);
+  const int s2 = cuna2_batch_set_schedule(p, best_lt, best_gm);
+  {
+    std::lock_guard<std::mutex> lk(p->mu);
+    p->use_graph = graph;
+  }
+  if (status) return status;
+  if (s2) return s2;
+  if (best_ms) *best_ms = best;
+  return CUNA2_SUCCESS;
 }

@@ -92,6 +92,7 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 // Launch with programmatic stream serialization: the kernel may start while
 // its predecessor finishes and waits for it with pdl_wait() (common.cuh).
 bool pdl_enabled();  // runtime.cu: false when the environment sets CUNA2_PDL=0
+void pdl_suppress(bool off);  // runtime.cu: this thread launches without it while `off`
 
 template <typename... KArgs, typename... Args>
 cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {

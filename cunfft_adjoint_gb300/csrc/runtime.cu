@@ -223,12 +223,18 @@ int *wait_timeout_counter() {
   return g_timeouts_dev;
 }
 
+namespace {
+thread_local bool g_pdl_off = false;
+}
+
+void pdl_suppress(bool off) { g_pdl_off = off; }
+
 bool pdl_enabled() {
   static const bool on = [] {
     const char *v = getenv("CUNA2_PDL");
     return !(v && v[0] == '0');
   }();
-  return on;
+  return on && !g_pdl_off;
 }
 
 bool masked_gather_forced() {

@@ -129,6 +129,33 @@ class AdjointNFFT:
             None if gt is None else gt.data_ptr(), t.numel(), float(t0), float(T), s or None))
         return gy, gt
 
+    def backward_batch(self, t, y, grad_F, t0, T, need_y=True, need_t=True, stream=None):
+        """(dL/dy, dL/dt) of B series at once: t, y (B, N), grad_F (B, nf),
+        t0 and T B values each (cuna2_adjoint_backward_batch)."""
+        import numpy as np
+        B = t.shape[0]
+        t = t.contiguous()
+        y = y.contiguous()
+        gy = torch.empty_like(y) if need_y else None
+        gt = torch.empty_like(t) if need_t else None
+        g = grad_F.contiguous()
+        if g.dtype != self.cdtype:
+            g = g.to(self.cdtype)
+        t0a = np.ascontiguousarray(np.broadcast_to(np.asarray(t0, np.float64), (B,)))
+        Ta = np.ascontiguousarray(np.broadcast_to(np.asarray(T, np.float64), (B,)))
+        s = (stream if stream is not None else torch.cuda.current_stream(t.device)).cuda_stream
+        _lib.check(_lib.core().cuna2_adjoint_backward_batch(
+            self._h, t.data_ptr(), y.data_ptr(), g.data_ptr(), None if gy is None else gy.data_ptr(),
+            None if gt is None else gt.data_ptr(), t.shape[1], B, t0a.ctypes.data, Ta.ctypes.data, s or None))
+        return gy, gt
+
+    def set_graph(self, enable=True):
+        """Replay each argument set's launch sequence as a CUDA graph
+        (cuna2_plan_set_graph): plain, bootstrap (reused across seeds) and
+        multi-channel calls."""
+        _lib.check(_lib.core().cuna2_plan_set_graph(self._h, 1 if enable else 0))
+        return self
+
     @property
     def schedule(self):
         """(log_tile, grid_method) of the tiled gridding."""
@@ -229,3 +256,23 @@ class BatchAdjointNFFT:
 
     def split(self, F):
         return [F[int(self.f_off[i]):int(self.f_off[i + 1])] for i in range(len(self.nf))]
+
+    @property
+    def schedule(self):
+        """(log_tile, grid_method) of the large series' gridding."""
+        lt, gm = ctypes.c_int(), ctypes.c_int()
+        _lib.check(_lib.core().cuna2_batch_get_schedule(self._h, ctypes.byref(lt), ctypes.byref(gm)))
+        return lt.value, gm.value
+
+    def set_schedule(self, log_tile, grid_method):
+        _lib.check(_lib.core().cuna2_batch_set_schedule(self._h, int(log_tile), int(grid_method)))
+
+    def autotune(self, t, y, reps=3, stream=None):
+        """Time every admissible schedule on (t, y), keep the fastest;
+        returns (log_tile, grid_method, best_ms)."""
+        out = torch.empty(int(self.f_off[-1]), dtype=self.cdtype, device=t.device)
+        s = (stream if stream is not None else torch.cuda.current_stream(t.device)).cuda_stream
+        ms = ctypes.c_float()
+        _lib.check(_lib.core().cuna2_batch_autotune(self._h, t.contiguous().data_ptr(), y.contiguous().data_ptr(),
+                                                    out.data_ptr(), s or None, int(reps), ctypes.byref(ms)))
+        return self.schedule + (ms.value,)

@@ -212,6 +212,17 @@ int cuna2_adjoint_backward(cuna2_plan plan, const double *t, const void *y, cons
                            void *grad_y, double *grad_t, int64_t n, double t0, double T,
                            cudaStream_t stream);
 
+/* cuna2_adjoint_backward for nseries series of n samples each on one plan
+ * (the training form: a batch of light curves per step).  Series s has times
+ * t[s*n .. (s+1)*n), values y[...], upstream gradient G[s*nf .. (s+1)*nf),
+ * its own t0[s] and T[s] (host arrays), and receives grad_y[s*n ..] and
+ * grad_t[s*n ..] (either may be NULL).  One launch per stage covers up to 256
+ * series; the plan's backward workspace grows to two packed complex grids
+ * per series of such a group.  No counterpart in the reference library. */
+int cuna2_adjoint_backward_batch(cuna2_plan plan, const double *t, const void *y, const void *G, void *grad_y,
+                                 double *grad_t, int64_t n, int nseries, const double *t0, const double *T,
+                                 cudaStream_t stream);
+
 /* Same transform with HOST arrays (pinned or pageable): copies t and y to
  * plan-owned device staging buffers, runs on `stream`, copies F back and
  * synchronises the stream before returning. */
@@ -229,19 +240,35 @@ int cuna2_adjoint_host(cuna2_plan plan, const double *t, const void *y, void *F,
 int cuna2_adjoint_host_async(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
                              double t0, double T, cudaStream_t stream);
 
-/* enable != 0: cuna2_adjoint / cuna2_adjoint_host capture their launch
- * sequence into a CUDA graph the first time they see an argument set
- * (pointers, n, t0, T) and replay it afterwards (up to 8 cached sets).  The
- * capture is taken on a private stream; the caller's stream only sees graph
- * launches. */
+/* enable != 0: cuna2_adjoint, cuna2_adjoint_host, cuna2_adjoint_bootstrap
+ * and cuna2_adjoint_multi capture their launch sequence into a CUDA graph the
+ * first time they see an argument set (pointers, n, t0, T, and the resample
+ * count and seed or the channel count) and replay it afterwards (up to 64
+ * cached sets, the oldest dropped first).  The capture is taken on a private
+ * stream; the caller's stream only sees graph launches. */
 int cuna2_plan_set_graph(cuna2_plan plan, int enable);
 
-/* Run one transform with CUDA events between its launches and return the
- * duration of each launch in milliseconds (stage_ms[0..*nstages)) and, if
- * stage_names is non-NULL, a static name for each.  Synchronises `stream`. */
+/* Per-launch durations of one transform: the launch sequence is captured with
+ * an event after every launch into a CUDA graph, launches serialised, and the
+ * graph is replayed once on `stream` (writing F), so each timestamp is taken
+ * on the device.  The first call on a plan, or one with more samples than
+ * before, runs the transform once eagerly beforehand to size the workspace.
+ * Returns the duration of
+ * each launch in milliseconds (stage_ms[0..*nstages)) and, if stage_names is
+ * non-NULL, a static name for each; the last entry, "event_gap", is the time
+ * between two event nodes with nothing between them, which every other
+ * entry includes once.  Synchronises `stream`. */
 int cuna2_plan_profile(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n,
                        double t0, double T, cudaStream_t stream, float *stage_ms,
                        const char **stage_names, int max_stages, int *nstages);
+
+/* The gridding kernel's own launch time: one transform of (t, y) into F in
+ * which the gridding launch (idempotent on the binned records) runs `reps`
+ * times back to back between two CUDA events on `stream`; *ms_per_launch
+ * receives the mean.  Tiled plans only (CUNA2_ERROR_UNSUPPORTED otherwise).
+ * Synchronises `stream`. */
+int cuna2_plan_time_grid(cuna2_plan plan, const double *t, const void *y, void *F, int64_t n, double t0,
+                         double T, int reps, cudaStream_t stream, float *ms_per_launch);
 
 /* Gridding schedule.  The grid is cut into tiles of 2^log_tile cells, one CTA
  * per tile staging it in shared memory and writing it to HBM once.  Forms:
@@ -324,6 +351,24 @@ int cuna2_batch_set_graph(cuna2_batch_plan plan, int enable);
 /* All transforms of the batch, stream-ordered. */
 int cuna2_batch_adjoint(cuna2_batch_plan plan, const double *t, const void *y, void *F,
                         cudaStream_t stream);
+
+/* Gridding schedule of the batch's large series (grids above the one-CTA
+ * size): tiles of 2^log_tile cells (10, 11 or 12) in CUNA2_GRID_FIXED form
+ * (bit-reproducible, the default, with 4096-cell tiles) or CUNA2_GRID_GATHER
+ * form.  Changing it rebuilds the plan's tables and workspace (synchronises
+ * the device, drops cached graphs). */
+int cuna2_batch_set_schedule(cuna2_batch_plan plan, int log_tile, int grid_method);
+int cuna2_batch_get_schedule(cuna2_batch_plan plan, int *log_tile, int *grid_method);
+
+/* Autotuner of a batched plan: runs the batch of (t, y) into F under every
+ * admissible schedule (both forms, log_tile 10..12), reps timed runs each
+ * (CUDA events on `stream`, minimum taken, a buffer of twice the L2 size
+ * overwritten before each run so the inputs come from HBM), and keeps the
+ * fastest; best_ms (may be NULL) receives its time.  Allocates and frees that
+ * buffer; synchronises the device.  No counterpart in the reference, whose
+ * batched API was never finished (src/cuna_kernel.cu:302-358). */
+int cuna2_batch_autotune(cuna2_batch_plan plan, const double *t, const void *y, void *F, cudaStream_t stream,
+                         int reps, float *best_ms);
 
 /* ---------------------------------------------------------------------- */
 /* integer steps read back (tests and diagnostics, not a transform path)   */

@@ -465,3 +465,88 @@ def test_unmasked_gather_matches_masked(tmp_path):
         res[tag] = np.load(tmp_path / (tag + ".npz"))
     for key in res["masked"].files:
         assert rel_l2(res["free"][key], res["masked"][key]) < 1e-6, key
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_graph_replay_of_bootstrap_and_channels(nfft, dtype):
+    """With graph replay on, a bootstrap graph is captured once per argument
+    set and replayed with a new draw seed each call (the draw kernel's seed
+    argument is updated in the instantiated graph); multi-channel calls are
+    replayed too.  Fixed-point gridding makes the grids bit-reproducible, so
+    replays must equal eager calls exactly, whatever order the seeds come in."""
+    from cunfft_adjoint_gb300 import _lib
+    rng = np.random.default_rng(13)
+    n, nf = 6000, 1 << 14
+    t = torch.as_tensor(rng.uniform(0, 50.0, n), device="cuda")
+    y = torch.as_tensor(rng.normal(0, 1, n), dtype=dtype, device="cuda")
+    Y = torch.stack([y, y * 0 + 1, y * y])
+    eager = nfft.AdjointNFFT(nf, 2, 8, dtype)
+    eager.set_schedule(11, _lib.GRID_FIXED)
+    want = {s: eager.bootstrap(t, y, 24, s, 0.0, 50.0).cpu().numpy() for s in (5, 6, 7)}
+    want_m = eager.multi(t, Y, 0.0, 50.0).cpu().numpy()
+    plan = nfft.AdjointNFFT(nf, 2, 8, dtype)
+    plan.set_schedule(11, _lib.GRID_FIXED)
+    plan.set_graph(True)
+    out = torch.empty((24, nf), dtype=plan.cdtype, device="cuda")
+    for s in (5, 6, 5, 7, 7, 6):
+        plan.bootstrap(t, y, 24, s, 0.0, 50.0, out=out)
+        assert np.array_equal(out.cpu().numpy(), want[s]), s
+    outm = torch.empty((3, nf), dtype=plan.cdtype, device="cuda")
+    for _ in range(2):
+        plan.multi(t, Y, 0.0, 50.0, out=outm)
+        assert np.array_equal(outm.cpu().numpy(), want_m)
+
+
+def test_profile_times_each_launch_on_the_device(nfft):
+    """cuna2_plan_profile replays the transform as a graph with an event node
+    after each launch: one positive duration per launch, F written, and the
+    durations stable from call to call (no host enqueue gaps)."""
+    import ctypes
+    from cunfft_adjoint_gb300 import _lib
+    rng = np.random.default_rng(17)
+    n, nf = 400_000, 1 << 19
+    t = torch.as_tensor(rng.uniform(0, 100.0, n), device="cuda")
+    y = torch.as_tensor(rng.normal(0, 1, n).astype(np.float32), device="cuda")
+    plan = nfft.AdjointNFFT(nf, 4, 12, torch.float32)
+    F = torch.empty(nf, dtype=torch.complex64, device="cuda")
+    ms = (ctypes.c_float * 16)()
+    names = (ctypes.c_char_p * 16)()
+    k = ctypes.c_int()
+    runs = []
+    for _ in range(5):
+        F.zero_()
+        _lib.check(_lib.core().cuna2_plan_profile(plan._h, t.data_ptr(), y.data_ptr(), F.data_ptr(), n, 0.0, 100.0,
+                                                  None, ms, names, 16, ctypes.byref(k)))
+        torch.cuda.synchronize()
+        runs.append({names[i].decode(): ms[i] for i in range(k.value)})
+    assert set(runs[0]) >= {"bin_count", "bin_scatter", "grid", "fft_colpass", "fft_rowpass", "event_gap"}
+    for r in runs:
+        assert all(v > 0 for key, v in r.items() if key != "event_gap") and r["event_gap"] >= 0
+    med = {key: float(np.median([r[key] for r in runs])) for key in runs[0]}
+    for r in runs[1:]:
+        for key, v in r.items():
+            assert abs(v - med[key]) < 0.5 * med[key] + 0.002, (key, v, med[key])
+    assert rel_l2(F.cpu().numpy(), plan(t, y, 0.0, 100.0).cpu().numpy()) < 1e-6
+
+
+def test_time_grid_launch(nfft):
+    """cuna2_plan_time_grid repeats the gridding launch of one transform back
+    to back between two events: a positive mean time, and the transform's
+    result unchanged by the repeats (the launch overwrites its grid)."""
+    import ctypes
+    from cunfft_adjoint_gb300 import _lib
+    rng = np.random.default_rng(19)
+    n, nf = 300_000, 1 << 19
+    t = torch.as_tensor(rng.uniform(0, 100.0, n), device="cuda")
+    y = torch.as_tensor(rng.normal(0, 1, n).astype(np.float32), device="cuda")
+    plan = nfft.AdjointNFFT(nf, 4, 12, torch.float32)
+    F = torch.empty(nf, dtype=torch.complex64, device="cuda")
+    ms = ctypes.c_float()
+    _lib.check(_lib.core().cuna2_plan_time_grid(plan._h, t.data_ptr(), y.data_ptr(), F.data_ptr(), n, 0.0, 100.0,
+                                                20, None, ctypes.byref(ms)))
+    assert 0 < ms.value < 1.0
+    assert rel_l2(F.cpu().numpy(), plan(t, y, 0.0, 100.0).cpu().numpy()) < 1e-6
+    small = nfft.AdjointNFFT(1024, 2, 8, torch.float32)
+    Fs = torch.empty(1024, dtype=torch.complex64, device="cuda")
+    assert _lib.core().cuna2_plan_time_grid(small._h, t.data_ptr(), y.data_ptr(), Fs.data_ptr(), 1000, 0.0, 100.0,
+                                            5, None, ctypes.byref(ms)) == 3

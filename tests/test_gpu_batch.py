@@ -121,3 +121,43 @@ def test_batch_with_empty_and_tiny_series(nfft, oracle_lib):
         k = np.arange(-nf[i] // 2, nf[i] // 2)[:: max(1, nf[i] // 256)]
         D = oracle_lib.ndft(ts[i], ys[i].astype(np.float64), 0.0, T[i], k)
         assert rel_l2(parts[i][k + nf[i] // 2], D) < 1e-5, i
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_batch_schedules_and_autotune(nfft, oracle_lib, dtype):
+    """Every schedule of a batched plan (tiles of 1024, 2048 and 4096 cells,
+    gather and fixed-point forms) gives each series' NDFT spectrum, the
+    schedules agree with each other to rounding, and the batch autotuner
+    keeps one of them."""
+    from cunfft_adjoint_gb300 import _lib
+    rng = np.random.default_rng(29)
+    n, nf, T, ts, ys = _batch_case(rng, 20, 2000, 60000, 1 << 17)
+    yd_np = np.concatenate(ys).astype(np.float32 if dtype == torch.float32 else np.float64)
+    plan = nfft.BatchAdjointNFFT(n, nf, 2, 8, np.zeros(len(n)), T, dtype)
+    td = torch.as_tensor(np.concatenate(ts), device="cuda")
+    yd = torch.as_tensor(yd_np, device="cuda")
+    assert plan.schedule == (12, _lib.GRID_FIXED)
+    offs = np.concatenate([[0], np.cumsum(n)])
+    big = [i for i in range(len(n)) if nf[i] * 2 > (1 << 15)]
+    outs = {}
+    for gm in (_lib.GRID_FIXED, _lib.GRID_GATHER):
+        for lt in (10, 11, 12):
+            plan.set_schedule(lt, gm)
+            assert plan.schedule == (lt, gm)
+            F = plan.split(plan(td, yd).cpu().numpy().astype(np.complex128))
+            for i in big[:3]:
+                k = np.arange(-nf[i] // 2, nf[i] // 2)
+                sel = np.sort(rng.choice(k, 128, replace=False))
+                D = oracle_lib.ndft(ts[i], yd_np[offs[i]:offs[i + 1]].astype(np.float64), 0.0, T[i], sel)
+                assert rel_l2(F[i][sel + nf[i] // 2], D) < (1e-5 if dtype == torch.float32 else 5e-8), (lt, gm, i)
+            outs[(lt, gm)] = np.concatenate(F)
+    ref = outs[(12, _lib.GRID_FIXED)]
+    for key, F in outs.items():
+        assert rel_l2(F, ref) < (2e-6 if dtype == torch.float32 else 1e-13), key
+    with pytest.raises(_lib.CunaError):
+        plan.set_schedule(9, _lib.GRID_GATHER)
+    with pytest.raises(_lib.CunaError):
+        plan.set_schedule(11, _lib.GRID_SCATTER)
+    lt, gm, ms = plan.autotune(td, yd, reps=2)
+    assert (lt, gm) in outs and ms > 0
+    assert rel_l2(plan(td, yd).cpu().numpy(), ref) < (2e-6 if dtype == torch.float32 else 1e-13)
