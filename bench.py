@@ -760,10 +760,16 @@ def main():
     dom = "grid"  # the largest share of the transform in the launch lists (profiles/)
     peak, peak_kind = peaks()
     ach = sb.get(dom, 0) / (grid_ms * 1e-3) / 1e9
-    traffic = None
+    # DRAM bytes per gridding launch, from the one-pass ncu launch list of
+    # the same bench command with this stream count (profiles/)
+    traffic, traffic_src = None, None
     tfile = os.path.join(ROOT, "profiles", "traffic_large.json")
     if os.path.exists(tfile):
-        traffic = json.load(open(tfile)).get(dom)
+        tj = json.load(open(tfile))
+        entry = tj.get("streams_%d" % nstr)
+        if entry:
+            traffic = entry.get(dom)
+            traffic_src = "%s (%d streams)" % (tj.get("source", "profiles/traffic_large.json"), nstr)
     total_bytes = sum(sb[k] for k in stages if k in sb)
     kernels_per_step = len([k for k in stages if k != "start"])
 
@@ -897,7 +903,8 @@ def main():
             "single_stream": {"value": ws * 1000.0 / ms1, "ms_per_step": ms1},
             "roofline": {"bound": "hbm", "kernel": "grid (k_grid_acc, gather gridding)", "achieved": ach,
                          "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
-                         "traffic": traffic, "algorithmic_bytes": sb.get(dom, 0),
+                         "traffic": traffic, "traffic_source": traffic_src,
+                         "algorithmic_bytes": sb.get(dom, 0),
                          "kernel_ms": grid_ms,
                          "timing": "mean of 50 back-to-back launches of the gridding kernel on one transform's "
                                    "records, CUDA events on the plan's stream (cuna2_plan_time_grid), median of 5"},
