@@ -157,7 +157,7 @@ def stage_bytes(n, ng, nf, rec_bytes=16, elem=4):
     }
 
 
-def batched_legs(dev, steps, which=("bootstrap", "uneven"), plain=True):
+def batched_legs(dev, steps, which=("bootstrap", "uneven"), plain=True, batch_schedule=None, uneven_series=4096):
     """Batched forms: bootstrap (N=5000, 1024 resamples, Nf=32768, R=2, m=8)
     and an uneven batch (4096 series, N log-uniform in [100, 1e5], Nf =
     nextpow2(4N) capped at 2^18, R=2, m=8), float32, CUDA-graph replay.
@@ -215,7 +215,7 @@ def batched_legs(dev, steps, which=("bootstrap", "uneven"), plain=True):
     if "uneven" in which:
         # uneven batch (its own seeded stream)
         rng = np.random.default_rng(4)
-        ns = 4096
+        ns = uneven_series
         nser = np.exp(rng.uniform(np.log(100), np.log(1e5), ns)).astype(np.int64)
         nfs = np.minimum(2 ** np.ceil(np.log2(4 * nser)).astype(np.int64), 1 << 18)
         Ts = np.exp(rng.uniform(np.log(10), np.log(3000), ns))
@@ -223,8 +223,13 @@ def batched_legs(dev, steps, which=("bootstrap", "uneven"), plain=True):
         yy = rng.normal(0, 1, int(nser.sum())).astype(np.float32)
         bp = BatchAdjointNFFT(nser, nfs, 2, 8, np.zeros(ns), Ts, torch.float32, device=dev, graph=True)
         tdd, ydd = torch.as_tensor(tt, device=dev), torch.as_tensor(yy, device=dev)
-        # the batch's own autotuner picks the tile size and gridding form
-        blt, bgm, _ = bp.autotune(tdd, ydd, reps=3)
+        # the batch's own autotuner picks the tile size and gridding form,
+        # unless the caller fixes them (launch lists of one schedule)
+        if batch_schedule:
+            bp.set_schedule(*batch_schedule)
+            blt, bgm = bp.schedule
+        else:
+            blt, bgm, _ = bp.autotune(tdd, ydd, reps=3)
         FF = torch.empty(int(nfs.sum()), dtype=torch.complex64, device=dev)
         for i in range(3):
             bp(tdd, ydd, out=FF)
@@ -236,8 +241,8 @@ def batched_legs(dev, steps, which=("bootstrap", "uneven"), plain=True):
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / k
-        out["uneven"] = {"workload": "4096 series, N log-U[100,1e5] (total %d), Nf=nextpow2(4N)<=2^18, R=2, m=8"
-                         % int(nser.sum()), "value": ns * 1000.0 / ms, "unit": UNIT, "ms_per_call": ms, "calls": k,
+        out["uneven"] = {"workload": "%d series, N log-U[100,1e5] (total %d), Nf=nextpow2(4N)<=2^18, R=2, m=8"
+                         % (ns, int(nser.sum())), "value": ns * 1000.0 / ms, "unit": UNIT, "ms_per_call": ms, "calls": k,
                          "schedule": {"log_tile": blt, "grid_method": ["gather", "scatter", "fixed"][bgm]},
                          "graph": True}
         if not plain:
@@ -617,7 +622,14 @@ def main():
     ap.add_argument("--only", choices=["bootstrap", "uneven", "autograd"],
                     help="run one batched leg alone (no plain leg) and print its result")
     ap.add_argument("--nsets", type=int, default=NSETS, help="rotating input sets (default 16: 192 MB > L2)")
+    ap.add_argument("--batch-schedule", default=None, metavar="LOG_TILE,FORM",
+                    help="uneven leg: this schedule (e.g. 12,fixed) instead of the batch autotuner")
+    ap.add_argument("--uneven-series", type=int, default=4096,
+                    help="uneven leg: number of series (fewer for small profiler captures)")
     args = ap.parse_args()
+    if args.batch_schedule:
+        lt_, gm_ = args.batch_schedule.split(",")
+        args.batch_schedule = (int(lt_), {"gather": 0, "scatter": 1, "fixed": 2}[gm_])
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         return reference_arm(args, wl)
@@ -625,7 +637,8 @@ def main():
         import torch
         dev = torch.device("cuda", 0)
         res = autograd_leg(dev, args.steps) if args.only == "autograd" else \
-            batched_legs(dev, args.steps, (args.only,), plain=False)[args.only]
+            batched_legs(dev, args.steps, (args.only,), plain=False, batch_schedule=args.batch_schedule,
+                         uneven_series=args.uneven_series)[args.only]
         print(json.dumps(res), flush=True)
         return
 

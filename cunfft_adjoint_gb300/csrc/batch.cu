@@ -701,7 +701,8 @@ extern "C" int cuna2_batch_set_schedule(cuna2_batch_plan p, int log_tile, int gr
   if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
   if (grid_method != CUNA2_GRID_GATHER && grid_method != CUNA2_GRID_FIXED)
     return fail(CUNA2_ERROR_INVALID_VALUE, "batched plans grid in gather or fixed-point form");
-  if (log_tile < 10 || log_tile > 12) return fail(CUNA2_ERROR_INVALID_VALUE, "log_tile must be 10, 11 or 12");
+  if (log_tile < 10 || log_tile > (grid_method == CUNA2_GRID_FIXED ? 13 : 12))
+    return fail(CUNA2_ERROR_INVALID_VALUE, "log_tile must be 10 to 13 (fixed point) or 10 to 12 (gather)");
   if (2 * p->m > (1 << log_tile)) return fail(CUNA2_ERROR_INVALID_VALUE, "tiles must span at least 2m cells");
   std::lock_guard<std::mutex> lk(p->mu);
   if (p->log_tile == log_tile && p->grid_method == grid_method) return CUNA2_SUCCESS;
@@ -751,7 +752,7 @@ extern "C" int cuna2_batch_autotune(cuna2_batch_plan p, const double *t, const v
   float best = 1e30f;
   int best_lt = p->log_tile, best_gm = p->grid_method, status = CUNA2_SUCCESS;
   for (int gm : {CUNA2_GRID_FIXED, CUNA2_GRID_GATHER}) {
-    for (int lt = 10; lt <= 12; ++lt) {
+    for (int lt = 10; lt <= (gm == CUNA2_GRID_FIXED ? 13 : 12); ++lt) {
       if (2 * p->m > (1 << lt)) continue;
       if (cuna2_batch_set_schedule(p, lt, gm) != CUNA2_SUCCESS) continue;
       float ms = 1e30f;

@@ -353,15 +353,16 @@ int cuna2_batch_adjoint(cuna2_batch_plan plan, const double *t, const void *y, v
                         cudaStream_t stream);
 
 /* Gridding schedule of the batch's large series (grids above the one-CTA
- * size): tiles of 2^log_tile cells (10, 11 or 12) in CUNA2_GRID_FIXED form
- * (bit-reproducible, the default, with 4096-cell tiles) or CUNA2_GRID_GATHER
- * form.  Changing it rebuilds the plan's tables and workspace (synchronises
+ * size): tiles of 2^log_tile cells in CUNA2_GRID_FIXED form (log_tile 10 to
+ * 13; bit-reproducible, the default, with 4096-cell tiles) or
+ * CUNA2_GRID_GATHER form (log_tile 10 to 12).  Changing it rebuilds the plan's tables and workspace (synchronises
  * the device, drops cached graphs). */
 int cuna2_batch_set_schedule(cuna2_batch_plan plan, int log_tile, int grid_method);
 int cuna2_batch_get_schedule(cuna2_batch_plan plan, int *log_tile, int *grid_method);
 
 /* Autotuner of a batched plan: runs the batch of (t, y) into F under every
- * admissible schedule (both forms, log_tile 10..12), reps timed runs each
+ * admissible schedule (fixed point with log_tile 10..13, gather with
+ * 10..12), reps timed runs each
  * (CUDA events on `stream`, minimum taken, a buffer of twice the L2 size
  * overwritten before each run so the inputs come from HBM), and keeps the
  * fastest; best_ms (may be NULL) receives its time.  Allocates and frees that

@@ -249,6 +249,31 @@ def test_fixed_point_grid_is_reproducible(nfft, dtype):
     assert torch.isnan(F3.real).any()
 
 
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_fixed_point_single_read_tiles(nfft, oracle_lib, dtype):
+    """Fixed-point tiles of one slab with at most 1024 (float) / 512 (double)
+    records stage them, build the bucket histogram and bound |y| in one read;
+    denser tiles and weighted slabs (multi-channel) take the chunked path.
+    Sparse samples with one dense burst give tiles of both kinds; channel 0
+    of a multi-channel transform with values [y, 2y] runs the chunked path on
+    the same records, so it must reproduce the plain transform's bits."""
+    from cunfft_adjoint_gb300 import _lib
+    rng = np.random.default_rng(41)
+    nf, T = 1 << 17, 100.0
+    t = np.concatenate([rng.uniform(0, T, 20_000), rng.uniform(40.0, 40.5, 6000)])
+    y = rng.normal(0, 1, t.size)
+    td = torch.as_tensor(t, device="cuda")
+    yd = torch.as_tensor(y, dtype=dtype, device="cuda")
+    plan = nfft.AdjointNFFT(nf, 2, 8, dtype)
+    plan.set_schedule(12, _lib.GRID_FIXED)
+    F = plan(td, yd, 0.0, T).clone()
+    M = plan.multi(td, torch.stack([yd, 2 * yd]), 0.0, T)
+    assert torch.equal(M[0], F)
+    sel = np.sort(rng.choice(np.arange(-nf // 2, nf // 2), 128, replace=False))
+    D = oracle_lib.ndft(t, yd.cpu().numpy().astype(np.float64), 0.0, T, sel)
+    assert rel_l2(F.cpu().numpy().astype(np.complex128)[sel + nf // 2], D) < (1e-5 if dtype == torch.float32 else 5e-8)
+
+
 def test_host_async_two_streams(nfft):
     """cuna2_adjoint_host_async from pinned host arrays, two plans on two
     streams in flight together, equals the device-array transform."""

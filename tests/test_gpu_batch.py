@@ -125,8 +125,8 @@ def test_batch_with_empty_and_tiny_series(nfft, oracle_lib):
 
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
 def test_batch_schedules_and_autotune(nfft, oracle_lib, dtype):
-    """Every schedule of a batched plan (tiles of 1024, 2048 and 4096 cells,
-    gather and fixed-point forms) gives each series' NDFT spectrum, the
+    """Every schedule of a batched plan (tiles of 1024 to 8192 cells in
+    fixed-point form, 1024 to 4096 in gather form) gives each series' NDFT spectrum, the
     schedules agree with each other to rounding, and the batch autotuner
     keeps one of them."""
     from cunfft_adjoint_gb300 import _lib
@@ -141,7 +141,7 @@ def test_batch_schedules_and_autotune(nfft, oracle_lib, dtype):
     big = [i for i in range(len(n)) if nf[i] * 2 > (1 << 15)]
     outs = {}
     for gm in (_lib.GRID_FIXED, _lib.GRID_GATHER):
-        for lt in (10, 11, 12):
+        for lt in ((10, 11, 12, 13) if gm == _lib.GRID_FIXED else (10, 11, 12)):
             plan.set_schedule(lt, gm)
             assert plan.schedule == (lt, gm)
             F = plan.split(plan(td, yd).cpu().numpy().astype(np.complex128))
@@ -158,6 +158,10 @@ def test_batch_schedules_and_autotune(nfft, oracle_lib, dtype):
         plan.set_schedule(9, _lib.GRID_GATHER)
     with pytest.raises(_lib.CunaError):
         plan.set_schedule(11, _lib.GRID_SCATTER)
+    with pytest.raises(_lib.CunaError):
+        plan.set_schedule(13, _lib.GRID_GATHER)
+    with pytest.raises(_lib.CunaError):
+        plan.set_schedule(14, _lib.GRID_FIXED)
     lt, gm, ms = plan.autotune(td, yd, reps=2)
     assert (lt, gm) in outs and ms > 0
     assert rel_l2(plan(td, yd).cpu().numpy(), ref) < (2e-6 if dtype == torch.float32 else 1e-13)
