@@ -756,6 +756,32 @@ __device__ __forceinline__ float fixed_stage(const Src &recs, int c0, int cnt,
   return ym;
 }
 
+// clear a fixed-point tile of TL cells (TL a multiple of 4, acc 16-byte
+// aligned) with 16-byte stores
+template <typename A> __device__ __forceinline__ void fixed_clear(A *acc, int TL) {
+  int4 *v = reinterpret_cast<int4 *>(acc);
+  const int nv = TL * (int)sizeof(A) / 16;
+  for (int i = threadIdx.x; i < nv; i += kGridThreads) v[i] = make_int4(0, 0, 0, 0);
+}
+// cells [i, i + 4) of a fixed-point tile as values: 16-byte shared loads
+__device__ __forceinline__ void fixed_load4(const int *acc, int i, float inv, float &a, float &b, float &c,
+                                            float &d) {
+  const int4 v = *reinterpret_cast<const int4 *>(acc + i);
+  a = (float)v.x * inv;
+  b = (float)v.y * inv;
+  c = (float)v.z * inv;
+  d = (float)v.w * inv;
+}
+__device__ __forceinline__ void fixed_load4(const long long *acc, int i, double inv, double &a, double &b,
+                                            double &c, double &d) {
+  const longlong2 u = *reinterpret_cast<const longlong2 *>(acc + i);
+  const longlong2 v = *reinterpret_cast<const longlong2 *>(acc + i + 2);
+  a = (double)u.x * inv;
+  b = (double)u.y * inv;
+  c = (double)v.x * inv;
+  d = (double)v.y * inv;
+}
+
 // all 2m taps of the staged records srec[0, cnt) into the tile acc, scaled by sc
 template <typename T>
 __device__ __forceinline__ void fixed_taps(const SRec<T> *srec, int cnt, T sc, const AccParams<T> &e,
@@ -855,7 +881,7 @@ __device__ __forceinline__ void grid_tile_fixed(const Src &recs, int r0, int r1,
     // Three barriers per tile instead of six; same scale, same bits.
     constexpr int PER = CAP / kGridThreads;
     const int cnt = r1 - r0;
-    for (int i = threadIdx.x; i < TL; i += kGridThreads) acc[i] = 0;
+    fixed_clear(acc, TL);
     __syncthreads();
     typename RecOf<T>::type rc[PER];
 #pragma unroll
@@ -894,8 +920,11 @@ __device__ __forceinline__ void grid_tile_fixed(const Src &recs, int r0, int r1,
     __syncthreads();
     T *out = grid + (int64_t)sbeg * slab_stride + base;
     const T inv = sc > (T)0 ? (T)1 / sc : (sc == sc ? (T)0 : sc);
-    for (int i = 4 * threadIdx.x; i < TL; i += 4 * kGridThreads)
-      store4(out + i, (T)acc[i] * inv, (T)acc[i + 1] * inv, (T)acc[i + 2] * inv, (T)acc[i + 3] * inv);
+    for (int i = 4 * threadIdx.x; i < TL; i += 4 * kGridThreads) {
+      T a, b, c, d;
+      fixed_load4(acc, i, inv, a, b, c, d);
+      store4(out + i, a, b, c, d);
+    }
     return;
   }
   __syncthreads();
@@ -929,7 +958,7 @@ __device__ __forceinline__ void grid_tile_fixed(const Src &recs, int r0, int r1,
       ym = (isnan(u) || isnan(ym)) ? __int_as_float(0x7fffffff) : fmaxf(ym, u);
     }
     if (lane == 0) red[warp] = ym;
-    for (int i = threadIdx.x; i < TL; i += kGridThreads) acc[i] = 0;
+    fixed_clear(acc, TL);
     __syncthreads();
     if (threadIdx.x == 0) scale_s = fixed_scale<T>(red, hmax);
     __syncthreads();
@@ -948,8 +977,11 @@ __device__ __forceinline__ void grid_tile_fixed(const Src &recs, int r0, int r1,
     // fixed-order flush: cell = integer / scale
     T *out = grid + (int64_t)slab * slab_stride + base;
     const T inv = sc > (T)0 ? (T)1 / sc : (sc == sc ? (T)0 : sc);
-    for (int i = 4 * threadIdx.x; i < TL; i += 4 * kGridThreads)
-      store4(out + i, (T)acc[i] * inv, (T)acc[i + 1] * inv, (T)acc[i + 2] * inv, (T)acc[i + 3] * inv);
+    for (int i = 4 * threadIdx.x; i < TL; i += 4 * kGridThreads) {
+      T a, b, c, d;
+      fixed_load4(acc, i, inv, a, b, c, d);
+      store4(out + i, a, b, c, d);
+    }
   }
 }
 

@@ -652,6 +652,57 @@ extern "C" int cuna2_batch_plan_create(cuna2_batch_plan *plan, int dtype, int ns
   return CUNA2_SUCCESS;
 }
 
+// Filter-width schedule of a batch: for R = 2, 4, 8 the smallest m whose
+// Gaussian error exp(-pi m sqrt(1 - 1/R)) reaches tol (clamped at the plan
+// type's rounding), each candidate autotuned over its gridding schedules on
+// the caller's batch, the fastest kept.
+extern "C" int cuna2_batch_plan_create_auto(cuna2_batch_plan *plan, int dtype, int nseries, const int64_t *n,
+                                            const int64_t *nf, double tol, const double *t0, const double *T,
+                                            const double *t, const void *y, void *F, cudaStream_t st, int *R_out,
+                                            int *m_out) {
+  clear_error();
+  if (!plan || !t || !y || !F || !(tol > 0) || !(tol < 1)) return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
+  *plan = nullptr;
+  if (dtype != CUNA2_F32 && dtype != CUNA2_F64) return fail(CUNA2_ERROR_INVALID_VALUE, "dtype %d", dtype);
+  const double target = std::max(tol, dtype == CUNA2_F32 ? 1e-7 : 1e-15);
+  cuna2_batch_plan best = nullptr;
+  float best_ms = 3.4e38f;
+  int bR = 0, bm = 0, last = CUNA2_SUCCESS;
+  for (int R = 2; R <= 8; R *= 2) {
+    int m = (int)std::ceil(-std::log(target) / (kPi * std::sqrt(1.0 - 1.0 / R)));
+    m = std::max(m, 2);
+    if (m > 16) continue;
+    cuna2_batch_plan c = nullptr;
+    last = cuna2_batch_plan_create(&c, dtype, nseries, n, nf, R, m, t0, T);
+    if (last != CUNA2_SUCCESS) continue;  // e.g. a grid too large at this R
+    float ms = 0.f;
+    const int s = cuna2_batch_autotune(c, t, y, F, st, 3, &ms);
+    if (s != CUNA2_SUCCESS) {
+      cuna2_batch_plan_destroy(c);
+      if (best) cuna2_batch_plan_destroy(best);
+      return s;
+    }
+    if (ms < best_ms) {
+      if (best) cuna2_batch_plan_destroy(best);
+      best = c;
+      best_ms = ms;
+      bR = R;
+      bm = m;
+    } else {
+      cuna2_batch_plan_destroy(c);
+    }
+  }
+  if (!best) {
+    if (last != CUNA2_SUCCESS) return last;  // the message of the last failed candidate stands
+    return fail(CUNA2_ERROR_UNSUPPORTED, "no batch plan reaches tol=%g with m <= 16", tol);
+  }
+  clear_error();
+  *plan = best;
+  if (R_out) *R_out = bR;
+  if (m_out) *m_out = bm;
+  return CUNA2_SUCCESS;
+}
+
 extern "C" int cuna2_batch_plan_destroy(cuna2_batch_plan p) {
   clear_error();
   if (p) batch_free(p);

@@ -203,7 +203,36 @@ class BatchAdjointNFFT:
     ``t0``/``T`` (per series) define ``x = (t - t0)/T - 1/2``.
     """
 
-    def __init__(self, n, nf, R=2, m=8, t0=None, T=None, dtype=torch.float32, device=None, graph=False):
+    @classmethod
+    def for_tolerance(cls, n, nf, tol, t, y, t0=None, T=None, dtype=torch.float32, graph=False):
+        """The batch plan (R, m, gridding schedule) that reaches relative error
+        `tol` fastest on the representative batch (t, y)
+        (cuna2_batch_plan_create_auto)."""
+        import numpy as np
+        self = cls.__new__(cls)
+        self._setup(n, nf, dtype, t.device)
+        if t.dtype != torch.float64 or y.dtype != dtype or t.numel() != int(self.n.sum()) or y.numel() != t.numel():
+            raise ValueError("t (float64) and y (plan dtype) must hold the batch's concatenated samples")
+        t, y = t.contiguous(), y.contiguous()
+        ns = len(self.n)
+        t0a = None if t0 is None else np.ascontiguousarray(t0, dtype=np.float64)
+        Ta = None if T is None else np.ascontiguousarray(T, dtype=np.float64)
+        out = torch.empty(int(self.nf.sum()), dtype=self.cdtype, device=t.device)
+        R, m = ctypes.c_int(), ctypes.c_int()
+        s = torch.cuda.current_stream(t.device).cuda_stream
+        self._h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.core().cuna2_batch_plan_create_auto(
+                ctypes.byref(self._h), _lib.F32 if dtype == torch.float32 else _lib.F64, ns,
+                self.n.ctypes.data, self.nf.ctypes.data, float(tol),
+                None if t0a is None else t0a.ctypes.data, None if Ta is None else Ta.ctypes.data,
+                t.data_ptr(), y.data_ptr(), out.data_ptr(), s or None, ctypes.byref(R), ctypes.byref(m)))
+        self.R, self.m = R.value, m.value
+        if graph:
+            _lib.check(_lib.core().cuna2_batch_set_graph(self._h, 1))
+        return self
+
+    def _setup(self, n, nf, dtype, device):
         import numpy as np
         self.n = np.ascontiguousarray(n, dtype=np.int64)
         self.nf = np.ascontiguousarray(nf, dtype=np.int64)
@@ -212,6 +241,13 @@ class BatchAdjointNFFT:
         self.dtype = dtype
         self.cdtype = torch.complex64 if dtype == torch.float32 else torch.complex128
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.f_off = np.concatenate([[0], np.cumsum(self.nf)])
+        self.s_off = np.concatenate([[0], np.cumsum(self.n)])
+
+    def __init__(self, n, nf, R=2, m=8, t0=None, T=None, dtype=torch.float32, device=None, graph=False):
+        import numpy as np
+        self.R, self.m = int(R), int(m)
+        self._setup(n, nf, dtype, device)
         ns = len(self.n)
         t0a = None if t0 is None else np.ascontiguousarray(t0, dtype=np.float64)
         Ta = None if T is None else np.ascontiguousarray(T, dtype=np.float64)
@@ -219,12 +255,10 @@ class BatchAdjointNFFT:
         with torch.cuda.device(self.device):
             _lib.check(_lib.core().cuna2_batch_plan_create(
                 ctypes.byref(self._h), _lib.F32 if dtype == torch.float32 else _lib.F64, ns,
-                self.n.ctypes.data, self.nf.ctypes.data, int(R), int(m),
+                self.n.ctypes.data, self.nf.ctypes.data, self.R, self.m,
                 None if t0a is None else t0a.ctypes.data, None if Ta is None else Ta.ctypes.data))
         if graph:
             _lib.check(_lib.core().cuna2_batch_set_graph(self._h, 1))
-        self.f_off = np.concatenate([[0], np.cumsum(self.nf)])
-        self.s_off = np.concatenate([[0], np.cumsum(self.n)])
 
     def __del__(self):
         h = getattr(self, "_h", None)

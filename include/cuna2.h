@@ -340,6 +340,17 @@ typedef struct cuna2_batch_plan_st *cuna2_batch_plan;
  * workspace up front. */
 int cuna2_batch_plan_create(cuna2_batch_plan *plan, int dtype, int nseries, const int64_t *n,
                             const int64_t *nf, int R, int m, const double *t0, const double *T);
+/* Filter-width schedule of a batch: like cuna2_plan_create_auto, for R = 2, 4,
+ * 8 the smallest m with exp(-pi m sqrt(1 - 1/R)) <= tol (tol clamped at 1e-7
+ * for float plans), each candidate batch plan autotuned by
+ * cuna2_batch_autotune on (t, y) (writing F), the fastest kept; R_out / m_out
+ * (may be NULL) receive the choice.  No counterpart in the reference, whose
+ * filter width is fixed and whose batched API was never finished
+ * (src/cuna_kernel.cu:302-358). */
+int cuna2_batch_plan_create_auto(cuna2_batch_plan *plan, int dtype, int nseries, const int64_t *n,
+                                 const int64_t *nf, double tol, const double *t0, const double *T,
+                                 const double *t, const void *y, void *F, cudaStream_t stream, int *R_out,
+                                 int *m_out);
 int cuna2_batch_plan_destroy(cuna2_batch_plan plan);
 /* Replace every series' t0/T (host arrays; synchronises the device). */
 int cuna2_batch_set_times(cuna2_batch_plan plan, const double *t0, const double *T);

@@ -16,10 +16,14 @@ def nfft(native_built):
     return N
 
 
-@pytest.mark.parametrize("n,nf,R,m,nbs", [(3000, 4096, 2, 8, 4), (20000, 65536, 2, 8, 3), (5000, 16384, 2, 8, 2)])
+@pytest.mark.parametrize("n,nf,R,m,nbs", [(3000, 4096, 2, 8, 4), (20000, 65536, 2, 8, 3), (5000, 16384, 2, 8, 2),
+                                           (5000, 32768, 2, 8, 3),
+                                           (4000, 16384, 4, 12, 2)])
 def test_bootstrap_resamples_vs_ndft(nfft, oracle_lib, n, nf, R, m, nbs):
     """Resample b uses samples d = xorshift32(wang_hash(seed + b*n + i)) % n
-    (the reference's draw stream) at their own times."""
+    (the reference's draw stream) at their own times: one-CTA plans (grids
+    of up to 32,768 cells) and tiled plans (65,536 and 131,072 cells), m = 8
+    and 12."""
     rng = np.random.default_rng(n)
     t = rng.uniform(0, 100.0, n)
     y = (np.sin(2 * np.pi * t / 2.1) + rng.normal(0, 0.3, n)).astype(np.float32)
@@ -165,3 +169,25 @@ def test_batch_schedules_and_autotune(nfft, oracle_lib, dtype):
     lt, gm, ms = plan.autotune(td, yd, reps=2)
     assert (lt, gm) in outs and ms > 0
     assert rel_l2(plan(td, yd).cpu().numpy(), ref) < (2e-6 if dtype == torch.float32 else 1e-13)
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-5), (torch.float64, 1e-9)])
+def test_batch_plan_for_tolerance(nfft, oracle_lib, dtype, tol):
+    """cuna2_batch_plan_create_auto picks (R, m) whose Gaussian error bound
+    meets the target and a gridding schedule by the batch autotuner; the
+    chosen plan's spectra meet the target against the FP64 NDFT."""
+    rng = np.random.default_rng(31)
+    n, nf, T, ts, ys = _batch_case(rng, 16, 100, 40000, 1 << 16)
+    y_np = np.concatenate(ys).astype(np.float32 if dtype == torch.float32 else np.float64)
+    td = torch.as_tensor(np.concatenate(ts), device="cuda")
+    yd = torch.as_tensor(y_np, device="cuda")
+    plan = nfft.BatchAdjointNFFT.for_tolerance(n, nf, tol, td, yd, np.zeros(len(n)), T, dtype)
+    assert plan.R in (2, 4, 8) and 2 <= plan.m <= 16
+    assert np.exp(-np.pi * plan.m * np.sqrt(1 - 1 / plan.R)) <= tol
+    F = plan.split(plan(td, yd).cpu().numpy().astype(np.complex128))
+    offs = np.concatenate([[0], np.cumsum(n)])
+    for i in range(0, len(n), 3):
+        k = np.arange(-nf[i] // 2, nf[i] // 2)[:: max(1, nf[i] // 128)]
+        D = oracle_lib.ndft(ts[i], y_np[offs[i]:offs[i + 1]].astype(np.float64), 0.0, T[i], k)
+        # float plans reach their rounding (a few 1e-7) on top of the kernel error
+        assert rel_l2(F[i][k + nf[i] // 2], D) < (1e-5 if dtype == torch.float32 else 5 * tol), i
