@@ -265,15 +265,26 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   const int nrb = resv ? (int)((n + rspan - 1) / rspan) : 0;
   // workspace: counts | cursor | offsets | phases or chunk table | reservations
   //            | records | grid slabs | weights
+  // With the reserved binning the phases and reservations are dead once the
+  // scatter pass has run, and the gridding writes the grid only after its
+  // grid-completion wait on that pass: they then share the grid's memory
+  // (when they fit), so a plan's intermediates take 10 MB less of L2 on the
+  // large workload and fewer dead lines are written back.
   const size_t o_cnt = 0, o_cur = align_up(sizeof(int) * ntiles), o_off = 2 * o_cur;
-  const size_t o_phs = o_off + align_up(sizeof(int) * (ntiles + 1));
+  const size_t o_hdr = o_off + align_up(sizeof(int) * (ntiles + 1));
   const size_t nrec = seg ? 2 * ((size_t)n + CH) : 2 * (size_t)(n > 0 ? n : 1);
-  const size_t o_rsv = o_phs + (small ? 0
-                                         : (seg ? align_up(sizeof(int) * (size_t)ntiles * nch)
-                                                : align_up(sizeof(uint64_t) * (size_t)(n > 0 ? n : 1))));
-  const size_t o_rec = o_rsv + (resv ? align_up(sizeof(int) * (size_t)nrb * ntiles) : 0);
-  const size_t o_grid = o_rec + (small ? 0 : align_up(sizeof(Rec) * nrec));
-  const size_t o_wts = o_grid + (small ? 0 : align_up(sizeof(T) * (size_t)p->ng * nslab));
+  const size_t phs_b = small ? 0
+                             : (seg ? align_up(sizeof(int) * (size_t)ntiles * nch)
+                                    : align_up(sizeof(uint64_t) * (size_t)(n > 0 ? n : 1)));
+  const size_t rsv_b = resv ? align_up(sizeof(int) * (size_t)nrb * ntiles) : 0;
+  const size_t rec_b = small ? 0 : align_up(sizeof(Rec) * nrec);
+  const size_t grid_b = small ? 0 : align_up(sizeof(T) * (size_t)p->ng * nslab);
+  const bool share = resv && phs_b + rsv_b <= grid_b;
+  const size_t o_phs = share ? o_hdr + rec_b : o_hdr;
+  const size_t o_rsv = o_phs + phs_b;
+  const size_t o_rec = share ? o_hdr : o_rsv + rsv_b;
+  const size_t o_grid = o_rec + rec_b;
+  const size_t o_wts = o_grid + grid_b;
   const size_t bytes = o_wts + (nbs > 0 ? sizeof(T) * (size_t)n * nbs : 0) + 256;
   void *ws = nullptr;
   CUNA_TRY(plan_workspace(p, bytes, &ws));
