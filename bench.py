@@ -189,9 +189,18 @@ def batched_legs(dev, steps, which=("bootstrap", "uneven"), plain=True, batch_sc
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / k
+        # algorithmic HBM bytes per call: draw weights written and read, t and y
+        # read, records written and read, each resample's real grid written,
+        # read and written by the column pass, read by the row pass, spectrum
+        # written (the grids of 1024 resamples, 268 MB, exceed L2)
+        ng = 2 * nf
+        bcall = 8 * n * nbs + 12 * n + 32 * n + nbs * (16 * ng + 8 * nf)
+        peak, pk = peaks()
         out["bootstrap"] = {"workload": "N=5000, 1024 resamples, Nf=32768, R=2, m=8", "value": nbs * 1000.0 / ms,
                             "unit": UNIT, "ms_per_call": ms, "calls": k,
-                            "graph": "one captured graph per argument set, a new draw seed every call"}
+                            "graph": "one captured graph per argument set, a new draw seed every call",
+                            "hbm": {"algorithmic_bytes_per_call": bcall, "gbs": bcall / ms / 1e6,
+                                    "frac_of_peak": bcall / ms / 1e6 / peak, "peak": peak, "peak_kind": pk}}
         if plain:
             # plain per-resample path: one single-series transform per resample
             # (resampled inputs prepared outside the timed region)
@@ -241,10 +250,19 @@ def batched_legs(dev, steps, which=("bootstrap", "uneven"), plain=True, batch_sc
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / k
+        # algorithmic HBM bytes per call: every series reads t and y and writes
+        # its spectrum; series with grids above 2^15 cells (the one-CTA limit)
+        # also write and read their records, write their grid, read and write
+        # it in the column pass and read it in the row pass
+        big = 2 * nfs > (1 << 15)
+        bcall = int((12 * nser + 8 * nfs).sum() + (32 * nser[big] + 16 * 2 * nfs[big]).sum())
+        peak, pk = peaks()
         out["uneven"] = {"workload": "%d series, N log-U[100,1e5] (total %d), Nf=nextpow2(4N)<=2^18, R=2, m=8"
                          % (ns, int(nser.sum())), "value": ns * 1000.0 / ms, "unit": UNIT, "ms_per_call": ms, "calls": k,
                          "schedule": {"log_tile": blt, "grid_method": ["gather", "scatter", "fixed"][bgm]},
-                         "graph": True}
+                         "graph": True,
+                         "hbm": {"algorithmic_bytes_per_call": bcall, "gbs": bcall / ms / 1e6,
+                                 "frac_of_peak": bcall / ms / 1e6 / peak, "peak": peak, "peak_kind": pk}}
         if not plain:
             return out
         # plain per-series path: one single-series plan call per series (plans
