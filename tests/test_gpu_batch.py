@@ -191,3 +191,64 @@ def test_batch_plan_for_tolerance(nfft, oracle_lib, dtype, tol):
         D = oracle_lib.ndft(ts[i], y_np[offs[i]:offs[i + 1]].astype(np.float64), 0.0, T[i], k)
         # float plans reach their rounding (a few 1e-7) on top of the kernel error
         assert rel_l2(F[i][k + nf[i] // 2], D) < (1e-5 if dtype == torch.float32 else 5 * tol), i
+
+
+def test_uneven_batch_full_size(nfft, oracle_lib):
+    """The uneven workload at its full size (4096 series, N log-uniform in
+    [100, 1e5], Nf = nextpow2(4N) capped at 2^18, R = 2, m = 8; about 61 M
+    samples) under the batch's autotuned schedule: 12 series spread over the
+    size range against the FP64 NDFT at 128 frequencies each, and linearity
+    (the batch of 2y + 1 equals twice the batch of y plus the batch of ones)
+    over every output."""
+    rng = np.random.default_rng(4)
+    ns = 4096
+    n = np.exp(rng.uniform(np.log(100), np.log(1e5), ns)).astype(np.int64)
+    nf = np.minimum(2 ** np.ceil(np.log2(4 * n)).astype(np.int64), 1 << 18)
+    T = np.exp(rng.uniform(np.log(10), np.log(3000), ns))
+    offs = np.concatenate([[0], np.cumsum(n)])
+    t = np.concatenate([rng.uniform(0, T[i], n[i]) for i in range(ns)])
+    y = rng.normal(0, 1, int(n.sum())).astype(np.float32)
+    plan = nfft.BatchAdjointNFFT(n, nf, 2, 8, np.zeros(ns), T, torch.float32)
+    td, yd = torch.as_tensor(t, device="cuda"), torch.as_tensor(y, device="cuda")
+    plan.autotune(td, yd, reps=1)
+    F = plan(td, yd).clone()
+    order = np.argsort(n)
+    pick = order[np.linspace(0, ns - 1, 12).astype(int)]
+    parts = plan.split(F)
+    for i in pick:
+        k = np.sort(rng.choice(np.arange(-nf[i] // 2, nf[i] // 2), 128, replace=False))
+        D = oracle_lib.ndft(t[offs[i]:offs[i + 1]], y[offs[i]:offs[i + 1]].astype(np.float64), 0.0, T[i], k)
+        assert rel_l2(parts[i].cpu().numpy()[k + nf[i] // 2], D) < 1e-5, (i, n[i])
+    G = plan(td, 2 * yd + 1).clone()
+    G -= 2 * F
+    G -= plan(td, torch.ones_like(yd))
+    # G now holds the linearity residual; relative to the batch of 2y + 1
+    res = float(torch.linalg.vector_norm(G)) / float(torch.linalg.vector_norm(plan(td, 2 * yd + 1)))
+    assert res < 1e-5, res
+
+
+def test_bootstrap_full_size(nfft, oracle_lib):
+    """The bootstrap workload at its full size (N = 5000, 1024 resamples,
+    Nf = 32768, R = 2, m = 8) under graph replay: 8 resamples spread over the
+    batch against the FP64 NDFT of the resampled series at 256 frequencies,
+    and every resample's spectrum equal to the single-resample bootstrap
+    computed on its own (the same draws)."""
+    rng = np.random.default_rng(3)
+    n, nbs, nf, seed = 5000, 1024, 32768, 77
+    t = rng.uniform(0, 100.0, n)
+    y = (np.sin(2 * np.pi * t / 2.1) + rng.normal(0, 0.3, n)).astype(np.float32)
+    td, yd = torch.as_tensor(t, device="cuda"), torch.as_tensor(y, device="cuda")
+    plan = nfft.AdjointNFFT(nf, 2, 8, torch.float32)
+    plan.set_graph(True)
+    F = plan.bootstrap(td, yd, nbs, seed, 0.0, 100.0).cpu().numpy()
+    draws = oracle_lib.bootstrap_draws_all(seed, n, nbs)
+    k = np.sort(rng.choice(np.arange(-nf // 2, nf // 2), 256, replace=False))
+    for b in np.linspace(0, nbs - 1, 8).astype(int):
+        d = draws[b]
+        D = oracle_lib.ndft(t[d], y[d].astype(np.float64), 0.0, 100.0, k)
+        assert rel_l2(F[b, k + nf // 2].astype(np.complex128), D) < 1e-5, b
+    # resample b of a seed is resample 0 of the seed advanced by b * n draws
+    one = nfft.AdjointNFFT(nf, 2, 8, torch.float32)
+    for b in (1, 511, 1023):
+        Fb = one.bootstrap(td, yd, 1, (seed + b * n) & 0xFFFFFFFF, 0.0, 100.0).cpu().numpy()
+        assert rel_l2(Fb[0], F[b]) < 1e-6, b
