@@ -20,12 +20,16 @@ template <int LOG1> __host__ __device__ constexpr int ct_pair_row(int p, int hal
   return half ? (p == 0 ? (1 << LOG1) / 2 : (1 << LOG1) - p) : p;
 }
 
-template <typename T, int LOG1, int LOG2> struct CtPairSrc {
+// Sequence seq of the CTA's buffer holds row ct_pair_row(p0 + i, half) with
+// seq = half P + i (first rows k1 of the CTA's slots, then their partners), so
+// that the epilogue's lanes, which take consecutive slots i, read rows one
+// odd pitch apart: conflict-free 8-byte shared loads.
+template <typename T, int LOG1, int LOG2, int LOGP> struct CtPairSrc {
   const typename CxOf<T>::type *p;  // slab
   int p0;
   __device__ __forceinline__ typename CxOf<T>::type load(int seq, int j, int dr) const {
     // through L2: the column pass may still have been writing when this kernel started
-    return __ldcg(p + (ct_pair_row<LOG1>(p0 + (seq >> 1), seq & 1) << LOG2) + j + dr);
+    return __ldcg(p + (ct_pair_row<LOG1>(p0 + (seq & ((1 << LOGP) - 1)), seq >> LOGP) << LOG2) + j + dr);
   }
 };
 
@@ -58,7 +62,7 @@ __device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *sl
     twr[u] = cmk(cs, sn);  // twr[B + k2] is twc[k2]
   }
   pdl_wait();  // the rows come from the column pass
-  CtPairSrc<T, LOG1, LOG2> src{slab, p0};
+  CtPairSrc<T, LOG1, LOG2, LOGP> src{slab, p0};
   ct_fft<T, LOG2, LOGB, false, false, false>(s, f.tw2, src, CtNoDst());
 #pragma unroll 4
   for (int idx = threadIdx.x; idx < (B << LOG2); idx += THREADS) {
@@ -70,8 +74,8 @@ __device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *sl
     // Z[L - k] is in row (L1 - k1) mod L1: the slot's other row, or the
     // same row for the self-paired rows 0 and L1/2 of slot 0
     const int k2m = k1 == 0 ? ((L2 - k2) & (L2 - 1)) : (L2 - 1 - k2);
-    const int seqm = p == 0 ? 2 * i + half : 2 * i + 1 - half;
-    const C Zk = s[(2 * i + half) * PITCH + cpad16(k2)];
+    const int seqm = p == 0 ? half * P + i : (1 - half) * P + i;
+    const C Zk = s[(half * P + i) * PITCH + cpad16(k2)];
     const C Zm = cconj(s[seqm * PITCH + cpad16(k2m)]);
     acc_output_tw<T>(e, k, Zk, Zm, Fs, cmul(twr[2 * i + half], twc[k2]));
   }
