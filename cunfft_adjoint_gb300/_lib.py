@@ -85,6 +85,8 @@ CORE_SIGNATURES = {
     "cuna2_plan_time_grid": (_I, [_P, _P, _P, _P, _I64, _D, _D, _I, _P, _P]),
     "cuna2_batch_plan_create": (_I, [_P, _I, _I, _P, _P, _I, _I, _P, _P]),
     "cuna2_batch_plan_create_auto": (_I, [_P, _I, _I, _P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "cuna2_batch_plan_create_ex": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P]),
+    "cuna2_batch_get_filter": (_I, [_P, _P, _P]),
     "cuna2_batch_plan_destroy": (_I, [_P]),
     "cuna2_batch_set_times": (_I, [_P, _P, _P]),
     "cuna2_batch_info": (_I, [_P, _P, _P]),

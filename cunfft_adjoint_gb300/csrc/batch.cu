@@ -272,8 +272,12 @@ template <typename V> int upload(const std::vector<V> &h, void **d) {
 }  // namespace cuna
 
 struct cuna2_batch_plan_st {
-  int dtype, R, m, nseries;
-  double tau;
+  int dtype, nseries;
+  int m_max;  // the widest filter of the batch (shared-memory sizes, tile spans)
+  std::vector<int> m_set;  // the batch's distinct filter widths
+  // oversampling and filter half-width of each series (cuna2_batch_plan_create_ex)
+  std::vector<int> R, m;
+  bool tail_free = true;  // every series' Gaussian tail allows the unmasked gather
   // gridding schedule of the large series (cuna2_batch_set_schedule)
   int log_tile = 12;
   int grid_method = CUNA2_GRID_FIXED;
@@ -334,12 +338,13 @@ template <typename T> int batch_build(cuna2_batch_plan_st *p) {
   int64_t s_off = 0, f_off = 0, g_off = 0;
   int tile0 = 0;
   for (int s = 0; s < p->nseries; ++s) {
-    const int64_t nf = p->nf[s], ng = nf * p->R, L = ng / 2;
+    const int64_t nf = p->nf[s], ng = nf * p->R[s], L = ng / 2;
     const int logL = ilog2i(L);
     const bool is_small = logL <= single_log;
     const int logTL = std::min(ilog2i(ng), p->log_tile);
     BDesc<T> &d = desc[s];
-    d.e = series_params<T>(nf, p->R, p->m, p->tau, logTL);
+    const double tau = (double)p->m[s] * p->R[s] / (4.0 * kPi * (p->R[s] - 0.5));
+    d.e = series_params<T>(nf, p->R[s], p->m[s], tau, logTL);
     d.pm = phase_setup(p->t0[s], p->T[s]);
     FftGeom g;
     CUNA_TRY(fft_geometry(dbl, logL, &g));
@@ -464,7 +469,7 @@ int batch_run(cuna2_batch_plan_st *p, const double *t, const T *y, typename CxOf
     for (size_t c = 0; c < p->small_classes.size(); ++c) {
       const int logL = p->small_classes[c].first, cnt = p->small_classes[c].second;
       const int L = 1 << logL;
-      const size_t smem = sizeof(C) * (size_t)fft_pitch(L, 1) + sizeof(T) * (2 * p->m + 2);
+      const size_t smem = sizeof(C) * (size_t)fft_pitch(L, 1) + sizeof(T) * (2 * p->m_max + 2);
       const int threads = std::max(32, std::min(1024, L / kFftE));
       k_bsmall<T><<<cnt, threads, smem, p->side>>>(t, y, D, (const int *)p->d_small_list + p->small_class_off[c], F);
       CUNA_CK(cudaGetLastError());
@@ -497,8 +502,8 @@ int batch_run(cuna2_batch_plan_st *p, const double *t, const T *y, typename CxOf
     const Rec *rc = (const Rec *)p->recs;
     const int *ts = (const int *)p->d_tile_series;
     if (p->grid_method == CUNA2_GRID_GATHER) {
-      const size_t smg = (grid_smem_bytes<T>(p->log_tile, p->m) + 15) & ~(size_t)15;
-      const bool free_ = tail_free_gather(sizeof(T) == 4, p->m, p->tau) && !masked_gather_forced();
+      const size_t smg = (grid_smem_bytes<T>(p->log_tile, p->m_max) + 15) & ~(size_t)15;
+      const bool free_ = sizeof(T) == 4 && p->tail_free && !masked_gather_forced();
       if (p->log_tile == 11) {
         if (free_) k_bgrid_gather<T, 8, false><<<ntl, kGridThreads, smg, st>>>(rc, p->offsets, (T *)p->grid, D, ts);
         else k_bgrid_gather<T, 8, true><<<ntl, kGridThreads, smg, st>>>(rc, p->offsets, (T *)p->grid, D, ts);
@@ -507,7 +512,10 @@ int batch_run(cuna2_batch_plan_st *p, const double *t, const T *y, typename CxOf
         else k_bgrid_gather<T, 4, true><<<ntl, kGridThreads, smg, st>>>(rc, p->offsets, (T *)p->grid, D, ts);
       }
     } else {
-      const size_t smg = grid_fixed_smem_bytes<T>(p->log_tile, p->m);
+      // the bucket table's length depends on m, not monotonically: the
+      // largest over the batch's filter widths
+      size_t smg = 0;
+      for (int mw : p->m_set) smg = std::max(smg, grid_fixed_smem_bytes<T>(p->log_tile, mw));
       k_bgrid<T><<<ntl, kGridThreads, smg, st>>>(rc, p->offsets, (T *)p->grid, D, ts);
     }
     CUNA_CK(cudaGetLastError());
@@ -614,18 +622,21 @@ template <typename T> void set_times_host(cuna2_batch_plan_st *p) {
 
 using namespace cuna;
 
-extern "C" int cuna2_batch_plan_create(cuna2_batch_plan *plan, int dtype, int nseries, const int64_t *n,
-                                       const int64_t *nf, int R, int m, const double *t0, const double *T) {
+extern "C" int cuna2_batch_plan_create_ex(cuna2_batch_plan *plan, int dtype, int nseries, const int64_t *n,
+                                          const int64_t *nf, const int *R, const int *m, const double *t0,
+                                          const double *T) {
   clear_error();
   if (!plan) return fail(CUNA2_ERROR_INVALID_VALUE, "plan pointer is NULL");
   *plan = nullptr;
   if (dtype != CUNA2_F32 && dtype != CUNA2_F64) return fail(CUNA2_ERROR_INVALID_VALUE, "dtype %d", dtype);
-  if (nseries < 1 || !n || !nf || R < 2 || m < 1 || m > 16)
-    return fail(CUNA2_ERROR_INVALID_VALUE, "need nseries >= 1, n and nf arrays, R >= 2, 1 <= m <= 16");
+  if (nseries < 1 || !n || !nf || !R || !m)
+    return fail(CUNA2_ERROR_INVALID_VALUE, "need nseries >= 1 and n, nf, R, m arrays");
   const int max_log = dtype == CUNA2_F32 ? 25 : 23;
   for (int s = 0; s < nseries; ++s) {
-    const int64_t ng = nf[s] * R, L = ng / 2;
-    if (n[s] < 0 || n[s] > ((int64_t)1 << 30) || nf[s] < 2 || (nf[s] & 1) || (L & (L - 1)) || ng < 4 * m ||
+    if (R[s] < 2 || m[s] < 1 || m[s] > 16)
+      return fail(CUNA2_ERROR_INVALID_VALUE, "series %d: need R >= 2 and 1 <= m <= 16 (R=%d m=%d)", s, R[s], m[s]);
+    const int64_t ng = nf[s] * R[s], L = ng / 2;
+    if (n[s] < 0 || n[s] > ((int64_t)1 << 30) || nf[s] < 2 || (nf[s] & 1) || (L & (L - 1)) || ng < 4 * m[s] ||
         ilog2i(L) > max_log)
       return fail(CUNA2_ERROR_INVALID_VALUE, "series %d: unsupported n=%lld nf=%lld (R*nf/2 must be a power of two)",
                   s, (long long)n[s], (long long)nf[s]);
@@ -633,10 +644,15 @@ extern "C" int cuna2_batch_plan_create(cuna2_batch_plan *plan, int dtype, int ns
   }
   cuna2_batch_plan_st *p = new cuna2_batch_plan_st();
   p->dtype = dtype;
-  p->R = R;
-  p->m = m;
   p->nseries = nseries;
-  p->tau = (double)m * R / (4.0 * kPi * (R - 0.5));
+  p->R.assign(R, R + nseries);
+  p->m.assign(m, m + nseries);
+  p->m_max = *std::max_element(m, m + nseries);
+  p->m_set.assign(m, m + nseries);
+  std::sort(p->m_set.begin(), p->m_set.end());
+  p->m_set.erase(std::unique(p->m_set.begin(), p->m_set.end()), p->m_set.end());
+  for (int s = 0; s < nseries; ++s)
+    p->tail_free = p->tail_free && tail_free_gather(true, m[s], (double)m[s] * R[s] / (4.0 * kPi * (R[s] - 0.5)));
   p->n.assign(n, n + nseries);
   p->nf.assign(nf, nf + nseries);
   p->t0.assign(nseries, 0.0);
@@ -652,45 +668,101 @@ extern "C" int cuna2_batch_plan_create(cuna2_batch_plan *plan, int dtype, int ns
   return CUNA2_SUCCESS;
 }
 
-// Filter-width schedule of a batch: for R = 2, 4, 8 the smallest m whose
+extern "C" int cuna2_batch_plan_create(cuna2_batch_plan *plan, int dtype, int nseries, const int64_t *n,
+                                       const int64_t *nf, int R, int m, const double *t0, const double *T) {
+  clear_error();
+  if (!plan) return fail(CUNA2_ERROR_INVALID_VALUE, "plan pointer is NULL");
+  *plan = nullptr;
+  if (nseries < 1 || !n || !nf || R < 2 || m < 1 || m > 16)
+    return fail(CUNA2_ERROR_INVALID_VALUE, "need nseries >= 1, n and nf arrays, R >= 2, 1 <= m <= 16");
+  const std::vector<int> Rs(nseries, R), ms(nseries, m);
+  return cuna2_batch_plan_create_ex(plan, dtype, nseries, n, nf, Rs.data(), ms.data(), t0, T);
+}
+
+extern "C" int cuna2_batch_get_filter(cuna2_batch_plan p, int *R, int *m) {
+  clear_error();
+  if (!p) return fail(CUNA2_ERROR_INVALID_VALUE, "NULL plan");
+  for (int s = 0; s < p->nseries; ++s) {
+    if (R) R[s] = p->R[s];
+    if (m) m[s] = p->m[s];
+  }
+  return CUNA2_SUCCESS;
+}
+
+// Filter-width schedule of a batch.  The candidates for each size class
+// (series of one output length nf) are R = 2, 4, 8 with the smallest m whose
 // Gaussian error exp(-pi m sqrt(1 - 1/R)) reaches tol (clamped at the plan
-// type's rounding), each candidate autotuned over its gridding schedules on
-// the caller's batch, the fastest kept.
+// type's rounding).  Every class starts at R = 2; then, class by class (most
+// samples first), R = 4 and 8 are tried with the other classes kept, each
+// candidate batch autotuned over its gridding schedules on the caller's
+// batch, and a class keeps the fastest.
 extern "C" int cuna2_batch_plan_create_auto(cuna2_batch_plan *plan, int dtype, int nseries, const int64_t *n,
                                             const int64_t *nf, double tol, const double *t0, const double *T,
                                             const double *t, const void *y, void *F, cudaStream_t st, int *R_out,
                                             int *m_out) {
   clear_error();
-  if (!plan || !t || !y || !F || !(tol > 0) || !(tol < 1)) return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
+  if (!plan || !n || !nf || nseries < 1 || !t || !y || !F || !(tol > 0) || !(tol < 1))
+    return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
   *plan = nullptr;
   if (dtype != CUNA2_F32 && dtype != CUNA2_F64) return fail(CUNA2_ERROR_INVALID_VALUE, "dtype %d", dtype);
   const double target = std::max(tol, dtype == CUNA2_F32 ? 1e-7 : 1e-15);
+  auto width = [&](int R) {
+    return std::max(2, (int)std::ceil(-std::log(target) / (kPi * std::sqrt(1.0 - 1.0 / R))));
+  };
+  // size classes by output length, most samples first
+  std::map<int64_t, int64_t> cls_n;
+  for (int s = 0; s < nseries; ++s) cls_n[nf[s]] += n[s];
+  std::vector<std::pair<int64_t, int64_t>> classes(cls_n.begin(), cls_n.end());
+  std::sort(classes.begin(), classes.end(), [](const std::pair<int64_t, int64_t> &a,
+                                              const std::pair<int64_t, int64_t> &b) { return a.second > b.second; });
+  std::map<int64_t, int> cls_R;
+  for (auto &c : classes) cls_R[c.first] = 2;
+  std::vector<int> Rs(nseries), ms(nseries);
   cuna2_batch_plan best = nullptr;
   float best_ms = 3.4e38f;
-  int bR = 0, bm = 0, last = CUNA2_SUCCESS;
-  for (int R = 2; R <= 8; R *= 2) {
-    int m = (int)std::ceil(-std::log(target) / (kPi * std::sqrt(1.0 - 1.0 / R)));
-    m = std::max(m, 2);
-    if (m > 16) continue;
+  int last = CUNA2_SUCCESS;
+  // builds and times the batch with the classes' current R; keeps it when faster
+  auto trial = [&](bool *kept) -> int {
+    *kept = false;
+    for (int s = 0; s < nseries; ++s) {
+      Rs[s] = cls_R[nf[s]];
+      ms[s] = width(Rs[s]);
+      if (ms[s] > 16) return CUNA2_SUCCESS;  // not reachable at this R
+    }
     cuna2_batch_plan c = nullptr;
-    last = cuna2_batch_plan_create(&c, dtype, nseries, n, nf, R, m, t0, T);
-    if (last != CUNA2_SUCCESS) continue;  // e.g. a grid too large at this R
-    float ms = 0.f;
-    const int s = cuna2_batch_autotune(c, t, y, F, st, 3, &ms);
+    last = cuna2_batch_plan_create_ex(&c, dtype, nseries, n, nf, Rs.data(), ms.data(), t0, T);
+    if (last != CUNA2_SUCCESS) return CUNA2_SUCCESS;  // e.g. a grid too large at this R
+    float ms_c = 0.f;
+    const int s = cuna2_batch_autotune(c, t, y, F, st, 3, &ms_c);
     if (s != CUNA2_SUCCESS) {
       cuna2_batch_plan_destroy(c);
-      if (best) cuna2_batch_plan_destroy(best);
       return s;
     }
-    if (ms < best_ms) {
+    if (ms_c < best_ms) {
       if (best) cuna2_batch_plan_destroy(best);
       best = c;
-      best_ms = ms;
-      bR = R;
-      bm = m;
+      best_ms = ms_c;
+      *kept = true;
     } else {
       cuna2_batch_plan_destroy(c);
     }
+    return CUNA2_SUCCESS;
+  };
+  bool kept = false;
+  int s = trial(&kept);
+  for (size_t ci = 0; !s && ci < classes.size(); ++ci) {
+    const int64_t key = classes[ci].first;
+    int keepR = cls_R[key];
+    for (int R = 4; !s && R <= 8; R *= 2) {
+      cls_R[key] = R;
+      s = trial(&kept);
+      if (kept) keepR = R;
+    }
+    cls_R[key] = keepR;
+  }
+  if (s) {
+    if (best) cuna2_batch_plan_destroy(best);
+    return s;
   }
   if (!best) {
     if (last != CUNA2_SUCCESS) return last;  // the message of the last failed candidate stands
@@ -698,8 +770,7 @@ extern "C" int cuna2_batch_plan_create_auto(cuna2_batch_plan *plan, int dtype, i
   }
   clear_error();
   *plan = best;
-  if (R_out) *R_out = bR;
-  if (m_out) *m_out = bm;
+  cuna2_batch_get_filter(best, R_out, m_out);
   return CUNA2_SUCCESS;
 }
 
@@ -754,7 +825,7 @@ extern "C" int cuna2_batch_set_schedule(cuna2_batch_plan p, int log_tile, int gr
     return fail(CUNA2_ERROR_INVALID_VALUE, "batched plans grid in gather or fixed-point form");
   if (log_tile < 10 || log_tile > (grid_method == CUNA2_GRID_FIXED ? 13 : 12))
     return fail(CUNA2_ERROR_INVALID_VALUE, "log_tile must be 10 to 13 (fixed point) or 10 to 12 (gather)");
-  if (2 * p->m > (1 << log_tile)) return fail(CUNA2_ERROR_INVALID_VALUE, "tiles must span at least 2m cells");
+  if (2 * p->m_max > (1 << log_tile)) return fail(CUNA2_ERROR_INVALID_VALUE, "tiles must span at least 2m cells");
   std::lock_guard<std::mutex> lk(p->mu);
   if (p->log_tile == log_tile && p->grid_method == grid_method) return CUNA2_SUCCESS;
   const int old_lt = p->log_tile, old_gm = p->grid_method;
@@ -804,7 +875,7 @@ extern "C" int cuna2_batch_autotune(cuna2_batch_plan p, const double *t, const v
   int best_lt = p->log_tile, best_gm = p->grid_method, status = CUNA2_SUCCESS;
   for (int gm : {CUNA2_GRID_FIXED, CUNA2_GRID_GATHER}) {
     for (int lt = 10; lt <= (gm == CUNA2_GRID_FIXED ? 13 : 12); ++lt) {
-      if (2 * p->m > (1 << lt)) continue;
+      if (2 * p->m_max > (1 << lt)) continue;
       if (cuna2_batch_set_schedule(p, lt, gm) != CUNA2_SUCCESS) continue;
       float ms = 1e30f;
       int s = cuna2_batch_adjoint(p, t, y, F, st);  // warm-up

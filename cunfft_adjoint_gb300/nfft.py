@@ -218,7 +218,7 @@ class BatchAdjointNFFT:
         t0a = None if t0 is None else np.ascontiguousarray(t0, dtype=np.float64)
         Ta = None if T is None else np.ascontiguousarray(T, dtype=np.float64)
         out = torch.empty(int(self.nf.sum()), dtype=self.cdtype, device=t.device)
-        R, m = ctypes.c_int(), ctypes.c_int()
+        R, m = np.zeros(ns, np.int32), np.zeros(ns, np.int32)
         s = torch.cuda.current_stream(t.device).cuda_stream
         self._h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
@@ -226,8 +226,8 @@ class BatchAdjointNFFT:
                 ctypes.byref(self._h), _lib.F32 if dtype == torch.float32 else _lib.F64, ns,
                 self.n.ctypes.data, self.nf.ctypes.data, float(tol),
                 None if t0a is None else t0a.ctypes.data, None if Ta is None else Ta.ctypes.data,
-                t.data_ptr(), y.data_ptr(), out.data_ptr(), s or None, ctypes.byref(R), ctypes.byref(m)))
-        self.R, self.m = R.value, m.value
+                t.data_ptr(), y.data_ptr(), out.data_ptr(), s or None, R.ctypes.data, m.ctypes.data))
+        self.R, self.m = R, m  # per series
         if graph:
             _lib.check(_lib.core().cuna2_batch_set_graph(self._h, 1))
         return self
@@ -245,17 +245,19 @@ class BatchAdjointNFFT:
         self.s_off = np.concatenate([[0], np.cumsum(self.n)])
 
     def __init__(self, n, nf, R=2, m=8, t0=None, T=None, dtype=torch.float32, device=None, graph=False):
+        """R and m: one value for every series, or one per series."""
         import numpy as np
-        self.R, self.m = int(R), int(m)
         self._setup(n, nf, dtype, device)
         ns = len(self.n)
+        self.R = np.ascontiguousarray(np.broadcast_to(np.asarray(R), (ns,)), dtype=np.int32)
+        self.m = np.ascontiguousarray(np.broadcast_to(np.asarray(m), (ns,)), dtype=np.int32)
         t0a = None if t0 is None else np.ascontiguousarray(t0, dtype=np.float64)
         Ta = None if T is None else np.ascontiguousarray(T, dtype=np.float64)
         self._h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
-            _lib.check(_lib.core().cuna2_batch_plan_create(
+            _lib.check(_lib.core().cuna2_batch_plan_create_ex(
                 ctypes.byref(self._h), _lib.F32 if dtype == torch.float32 else _lib.F64, ns,
-                self.n.ctypes.data, self.nf.ctypes.data, self.R, self.m,
+                self.n.ctypes.data, self.nf.ctypes.data, self.R.ctypes.data, self.m.ctypes.data,
                 None if t0a is None else t0a.ctypes.data, None if Ta is None else Ta.ctypes.data))
         if graph:
             _lib.check(_lib.core().cuna2_batch_set_graph(self._h, 1))

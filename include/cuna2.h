@@ -340,13 +340,25 @@ typedef struct cuna2_batch_plan_st *cuna2_batch_plan;
  * workspace up front. */
 int cuna2_batch_plan_create(cuna2_batch_plan *plan, int dtype, int nseries, const int64_t *n,
                             const int64_t *nf, int R, int m, const double *t0, const double *T);
-/* Filter-width schedule of a batch: like cuna2_plan_create_auto, for R = 2, 4,
- * 8 the smallest m with exp(-pi m sqrt(1 - 1/R)) <= tol (tol clamped at 1e-7
- * for float plans), each candidate batch plan autotuned by
- * cuna2_batch_autotune on (t, y) (writing F), the fastest kept; R_out / m_out
- * (may be NULL) receive the choice.  No counterpart in the reference, whose
- * filter width is fixed and whose batched API was never finished
- * (src/cuna_kernel.cu:302-358). */
+/* A batch plan with its own oversampling R[s] and filter half-width m[s] per
+ * series (host arrays of nseries ints; R[s] * nf[s] / 2 a power of two,
+ * 1 <= m[s] <= 16); otherwise as cuna2_batch_plan_create, which is this with
+ * one R and m for every series. */
+int cuna2_batch_plan_create_ex(cuna2_batch_plan *plan, int dtype, int nseries, const int64_t *n,
+                               const int64_t *nf, const int *R, const int *m, const double *t0,
+                               const double *T);
+/* R[s] and m[s] of every series (host arrays of nseries ints; either may be
+ * NULL). */
+int cuna2_batch_get_filter(cuna2_batch_plan plan, int *R, int *m);
+/* Filter-width schedule of a batch, per size class (the series of one output
+ * length nf): candidates R = 2, 4, 8 with the smallest m whose Gaussian error
+ * exp(-pi m sqrt(1 - 1/R)) <= tol (tol clamped at 1e-7 for float plans).  All
+ * classes start at R = 2; then, class by class (most samples first), R = 4
+ * and 8 are tried with the other classes kept, each candidate batch autotuned
+ * by cuna2_batch_autotune on (t, y) (writing F), and a class keeps the
+ * fastest.  R_out / m_out (host arrays of nseries ints, may be NULL) receive
+ * the choice.  No counterpart in the reference, whose filter width is fixed
+ * and whose batched API was never finished (src/cuna_kernel.cu:302-358). */
 int cuna2_batch_plan_create_auto(cuna2_batch_plan *plan, int dtype, int nseries, const int64_t *n,
                                  const int64_t *nf, double tol, const double *t0, const double *T,
                                  const double *t, const void *y, void *F, cudaStream_t stream, int *R_out,

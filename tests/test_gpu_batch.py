@@ -173,17 +173,21 @@ def test_batch_schedules_and_autotune(nfft, oracle_lib, dtype):
 
 @pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-5), (torch.float64, 1e-9)])
 def test_batch_plan_for_tolerance(nfft, oracle_lib, dtype, tol):
-    """cuna2_batch_plan_create_auto picks (R, m) whose Gaussian error bound
-    meets the target and a gridding schedule by the batch autotuner; the
-    chosen plan's spectra meet the target against the FP64 NDFT."""
+    """cuna2_batch_plan_create_auto picks (R, m) per size class whose
+    Gaussian error bound meets the target and a gridding schedule by the
+    batch autotuner; the chosen plan's spectra meet the target against the
+    FP64 NDFT."""
     rng = np.random.default_rng(31)
     n, nf, T, ts, ys = _batch_case(rng, 16, 100, 40000, 1 << 16)
     y_np = np.concatenate(ys).astype(np.float32 if dtype == torch.float32 else np.float64)
     td = torch.as_tensor(np.concatenate(ts), device="cuda")
     yd = torch.as_tensor(y_np, device="cuda")
     plan = nfft.BatchAdjointNFFT.for_tolerance(n, nf, tol, td, yd, np.zeros(len(n)), T, dtype)
-    assert plan.R in (2, 4, 8) and 2 <= plan.m <= 16
-    assert np.exp(-np.pi * plan.m * np.sqrt(1 - 1 / plan.R)) <= tol
+    assert np.all(np.isin(plan.R, (2, 4, 8))) and np.all((plan.m >= 2) & (plan.m <= 16))
+    assert np.all(np.exp(-np.pi * plan.m * np.sqrt(1 - 1 / plan.R)) <= tol)
+    # one (R, m) per size class
+    for v in np.unique(nf):
+        assert len(set(zip(plan.R[nf == v], plan.m[nf == v]))) == 1
     F = plan.split(plan(td, yd).cpu().numpy().astype(np.complex128))
     offs = np.concatenate([[0], np.cumsum(n)])
     for i in range(0, len(n), 3):
@@ -252,3 +256,32 @@ def test_bootstrap_full_size(nfft, oracle_lib):
     for b in (1, 511, 1023):
         Fb = one.bootstrap(td, yd, 1, (seed + b * n) & 0xFFFFFFFF, 0.0, 100.0).cpu().numpy()
         assert rel_l2(Fb[0], F[b]) < 1e-6, b
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_batch_per_series_filter_widths(nfft, oracle_lib, dtype):
+    """Series of one batch with their own (R, m) (2, 8), (4, 5), (8, 4), (4,
+    12) and (2, 16) over small and large grids, under every gridding form:
+    each series' spectrum matches the FP64 NDFT to ten times its own kernel
+    error bound (at least 1e-5 float, 1e-10 double)."""
+    from cunfft_adjoint_gb300 import _lib
+    rng = np.random.default_rng(37)
+    n, nf, T, ts, ys = _batch_case(rng, 20, 200, 40000, 1 << 16)
+    R = np.array([2, 4, 8, 4, 2] * 4)
+    m = np.array([8, 5, 4, 12, 16] * 4)
+    y_np = np.concatenate(ys).astype(np.float32 if dtype == torch.float32 else np.float64)
+    td = torch.as_tensor(np.concatenate(ts), device="cuda")
+    yd = torch.as_tensor(y_np, device="cuda")
+    plan = nfft.BatchAdjointNFFT(n, nf, R, m, np.zeros(len(n)), T, dtype)
+    offs = np.concatenate([[0], np.cumsum(n)])
+    for lt, gm in ((12, _lib.GRID_FIXED), (12, _lib.GRID_GATHER), (13, _lib.GRID_FIXED)):
+        plan.set_schedule(lt, gm)
+        F = plan.split(plan(td, yd).cpu().numpy().astype(np.complex128))
+        for i in range(len(n)):
+            k = np.arange(-nf[i] // 2, nf[i] // 2)[:: max(1, nf[i] // 128)]
+            D = oracle_lib.ndft(ts[i], y_np[offs[i]:offs[i + 1]].astype(np.float64), 0.0, T[i], k)
+            bound = np.exp(-np.pi * m[i] * np.sqrt(1 - 1 / R[i]))
+            # double plans also carry ~1e-11 beyond the Gaussian bound at
+            # m = 12, R = 4 (the single-series double tests allow 1e-9)
+            tol = max(10 * bound, 1e-5 if dtype == torch.float32 else 1e-10)
+            assert rel_l2(F[i][k + nf[i] // 2], D) < tol, (lt, gm, i, R[i], m[i])
