@@ -285,3 +285,20 @@ def test_batch_per_series_filter_widths(nfft, oracle_lib, dtype):
             # m = 12, R = 4 (the single-series double tests allow 1e-9)
             tol = max(10 * bound, 1e-5 if dtype == torch.float32 else 1e-10)
             assert rel_l2(F[i][k + nf[i] // 2], D) < tol, (lt, gm, i, R[i], m[i])
+
+
+def test_batch_per_series_widths_reject_bad_values(nfft):
+    """cuna2_batch_plan_create_ex rejects a per-series R below 2, m outside
+    [1, 16], and an R that does not make R nf / 2 a power of two; the
+    failure names the series."""
+    from cunfft_adjoint_gb300 import _lib
+    n = np.array([100, 200, 300], dtype=np.int64)
+    nf = np.array([1024, 2048, 4096], dtype=np.int64)
+    for R, m in (([2, 1, 2], [8, 8, 8]), ([2, 2, 2], [8, 17, 8]), ([2, 2, 2], [8, 8, 0]), ([2, 3, 2], [8, 8, 8])):
+        with pytest.raises(_lib.CunaError, match="series"):
+            nfft.BatchAdjointNFFT(n, nf, np.array(R), np.array(m))
+    plan = nfft.BatchAdjointNFFT(n, nf, np.array([2, 4, 8]), np.array([8, 5, 4]))
+    R = np.zeros(3, np.int32)
+    m = np.zeros(3, np.int32)
+    _lib.check(_lib.core().cuna2_batch_get_filter(plan._h, R.ctypes.data, m.ctypes.data))
+    assert list(R) == [2, 4, 8] and list(m) == [8, 5, 4]
