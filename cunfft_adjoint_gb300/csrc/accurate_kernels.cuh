@@ -733,7 +733,7 @@ __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 3) k_grid_s
 // reach one cell, hmax the largest count of records in a bucket of
 // max(2m, 16) consecutive cells (a cell's 2m-cell window meets two buckets);
 // weights are <= 1.  With the sum bounded by 2^30 (float, int32 cells) or
-// 2^62 (double, int64 cells) units, the quantum is 2^-30 (2^-62) of the
+// 2^50 (double, int64 cells) units, the quantum is 2^-30 (2^-50) of the
 // bound.  Integer sums do not depend on the order of the atomics, so the grid
 // is bit-reproducible run to run.  A non-finite value makes its tiles NaN.
 // records [c0, c0 + cnt) -> srec (values from ws when given); returns the

@@ -116,7 +116,12 @@ cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, 
 // Fixed-point accumulation in shared memory: a value w (already scaled so
 // that every cell's sum stays within `range`) is rounded to an integer and
 // added with a native shared-memory integer atomic; integer sums do not
-// depend on the order of the atomics.
+// depend on the order of the atomics.  Double cells round by adding
+// 1.5 * 2^52 (the integer lands in the low mantissa bits; exact round to
+// nearest for |w| < 2^51), one FP64 add that the multiply before it fuses
+// into, instead of a conversion on the FP64 pipe (gridding of the large
+// float64 workload 354 -> 299 us); hence the 2^50 range, a quantum of 2^-50
+// of each tile's bound.
 template <typename T> struct FixAcc;
 template <> struct FixAcc<float> {
   typedef int type;
@@ -126,8 +131,10 @@ template <> struct FixAcc<float> {
 };
 template <> struct FixAcc<double> {
   typedef long long type;
-  static constexpr double range = 4611686018427387904.0;  // 2^62
-  __device__ static long long to_fix(double w) { return __double2ll_rn(w); }
+  static constexpr double range = 1125899906842624.0;  // 2^50
+  __device__ static long long to_fix(double w) {
+    return __double_as_longlong(w + 6755399441055744.0) - 0x4338000000000000ll;
+  }
   __device__ static void add(long long *a, long long v) {
     atomicAdd(reinterpret_cast<unsigned long long *>(a), (unsigned long long)v);
   }

