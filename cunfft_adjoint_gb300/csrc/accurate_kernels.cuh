@@ -793,7 +793,12 @@ __device__ __forceinline__ void fixed_taps(const SRec<T> *srec, int cnt, T sc, c
   for (int i = threadIdx.x; i < cnt; i += kGridThreads) {
     const SRec<T> q = srec[i];
     const T E = q.y * sc * exp2_g(-e.k1 * q.f * q.f);
-    const T Q = exp2_g(e.k2 * q.f), Qi = exp2_g(-e.k2 * q.f);
+    const T Q = exp2_g(e.k2 * q.f);
+    // double: 1/Q by the FP64 reciprocal, a few FP64 operations instead of a
+    // third exp2; float keeps the hardware exp2
+    T Qi;
+    if constexpr (sizeof(T) == 8) Qi = __drcp_rn(Q);
+    else Qi = exp2_g(-e.k2 * q.f);
     const int p0 = q.lc;
     if (p0 - m + 1 >= 0 && p0 + m < TL) {  // every tap inside the tile
       A *a = acc + p0;
