@@ -47,6 +47,10 @@ struct cuna2_plan_st {
   bool has_split = false;
   bool tiled_single = true;
   cuna::FftGeom geom4;
+  // double plans with four-step passes: the float-float geometry the passes
+  // compute in (fft_geometry_df)
+  bool has_df = false;
+  cuna::FftGeom geom_df;
   cuna::FftGeom geom;
   int device;
   std::mutex mu;
@@ -142,8 +146,8 @@ inline void mark(Prof *pr, const char *name, cudaStream_t st) {
 // lengths that have an instance: returns 1 when launched, 0 when logL has no
 // instance, -1 on a launch error.
 template <typename T, int LOGL>
-int ct_passes_at(typename CxOf<T>::type *z, const FftDev<T> &f, const AccParams<T> &e, typename CxOf<T>::type *F,
-                 int nslab, cudaStream_t st, Prof *pr) {
+int ct_passes_at(typename MemOf<T>::type *z, const FftDev<T> &f, const AccParams<typename AccOf<T>::type> &e,
+                 typename MemOf<T>::type *F, int nslab, cudaStream_t st, Prof *pr) {
   constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
   constexpr int BA = PassCfg<T>::ELEMS >> LOG1;
   constexpr size_t smA = ct_colpass_smem<T, LOGL>(), smB = ct_rowpass_smem<T, LOGL>();
@@ -185,8 +189,8 @@ int ct_passes_at(typename CxOf<T>::type *z, const FftDev<T> &f, const AccParams<
 }
 
 template <typename T>
-int ct_passes(int logL, typename CxOf<T>::type *z, const FftDev<T> &f, const AccParams<T> &e,
-              typename CxOf<T>::type *F, int nslab, cudaStream_t st, Prof *pr) {
+int ct_passes(int logL, typename MemOf<T>::type *z, const FftDev<T> &f, const AccParams<typename AccOf<T>::type> &e,
+              typename MemOf<T>::type *F, int nslab, cudaStream_t st, Prof *pr) {
 #define CUNA_CT(LG) \
   case LG: return ct_passes_at<T, LG>(z, f, e, F, nslab, st, pr);
   if constexpr (sizeof(T) == 4) {
@@ -466,7 +470,17 @@ int adjoint_run(cuna2_plan_st *p, const double *t, const T *y, typename CxOf<T>:
   // packed complex view of the real grid slabs
   C *z = reinterpret_cast<C *>(grid);
   {
-    const int h = ct_passes<T>(p->geom.logL, z, f, e, F, nslab, st, pr);
+    int h;
+    if constexpr (sizeof(T) == 8) {
+      // double plans compute both passes in float-float (the FP32 pipe) and
+      // keep the grid and the spectrum in double
+      if (p->has_df && !fp64_passes_forced())
+        h = ct_passes<dfl>(p->geom.logL, z, to_dev<dfl>(p->geom_df), e, F, nslab, st, pr);
+      else
+        h = ct_passes<T>(p->geom.logL, z, f, e, F, nslab, st, pr);
+    } else {
+      h = ct_passes<T>(p->geom.logL, z, f, e, F, nslab, st, pr);
+    }
     if (h < 0) return fail_cuda(cudaGetLastError(), "FFT pass launch");
     if (h == 1) return CUNA2_SUCCESS;
   }
@@ -534,6 +548,11 @@ extern "C" int cuna2_plan_create(cuna2_plan *plan, int dtype, int64_t nf, int R,
   }
   p->has_split = p->small && logL >= (dtype == CUNA2_F32 ? 13 : 12);
   if (p->has_split && (st = fft_geometry(dtype == CUNA2_F64, logL, &p->geom4, true))) {
+    delete p;
+    return st;
+  }
+  p->has_df = dtype == CUNA2_F64 && !p->small && logL <= 23;
+  if (p->has_df && (st = fft_geometry_df(logL, &p->geom_df))) {
     delete p;
     return st;
   }

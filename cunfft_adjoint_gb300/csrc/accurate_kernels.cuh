@@ -98,18 +98,22 @@ __device__ __forceinline__ void acc_output(const AccParams<T> &e, int64_t k, typ
 
 // The same with the unpack twiddle exp(2 pi i k / ng) supplied (from tables)
 // and the deconvolution factor by exp2.
+// (float-float plans: the unpack in float-float, the deconvolution factor and
+// the output in double)
 template <typename T>
-__device__ __forceinline__ void acc_output_tw(const AccParams<T> &e, int64_t k, typename CxOf<T>::type Zk,
-                                              typename CxOf<T>::type Zmc, typename CxOf<T>::type *F,
-                                              typename CxOf<T>::type tw) {
+__device__ __forceinline__ void acc_output_tw(const AccParams<typename AccOf<T>::type> &e, int64_t k,
+                                              typename CxOf<T>::type Zk, typename CxOf<T>::type Zmc,
+                                              typename MemOf<T>::type *F, typename CxOf<T>::type tw) {
   typedef typename CxOf<T>::type C;
-  const C A = cadd(Zk, Zmc);
+  typedef typename AccOf<T>::type A;
+  typedef typename MemOf<T>::type M;
+  const C Ap = cadd(Zk, Zmc);
   const C Bv = cmuli(csub(Zmc, Zk));
-  const C G2 = cadd(A, cmul(tw, Bv));
-  const T kf = (T)(int)k;
-  T sc = e.c0 * exp2_t(e.c1 * (T)1.4426950408889634 * kf * kf);
+  const C G2 = cadd(Ap, cmul(tw, Bv));
+  const A kf = (A)(int)k;
+  A sc = e.c0 * exp2_t(e.c1 * (A)1.4426950408889634 * kf * kf);
   if (k & 1) sc = -sc;
-  const C Fk = cscale(G2, sc);
+  const M Fk = cscale(cx_to_mem(G2), sc);
   if (k < e.K) F[e.K + k] = Fk;
   if (k >= 1) F[e.K - k] = cconj(Fk);
 }

@@ -6,12 +6,83 @@
 
 namespace cuna {
 
+// Float-float ("double-float") scalar: an unevaluated sum hi + lo of two
+// floats, |lo| <= ulp(hi) / 2, about 48 significant bits.  The float64 plan's
+// FFT passes compute in it on the FP32 pipe (GB300's FP64 rate is a small
+// fraction of its FP32 rate) and keep double in memory.  Sums by Knuth's
+// two-sum, products by an FMA-exact product (Dekker's method with fma), both
+// renormalised by a fast two-sum (Dekker 1971; Hida, Li, Bailey 2001).
+struct dfl {
+  float hi, lo;
+  dfl() = default;
+  __host__ __device__ constexpr dfl(float h, float l) : hi(h), lo(l) {}
+  // from a double constant or value: the nearest float and the remainder
+  __host__ __device__ constexpr dfl(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+};
+__host__ __device__ __forceinline__ dfl df_fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return dfl(s, b - (s - a));
+}
+__host__ __device__ __forceinline__ dfl operator+(dfl a, dfl b) {
+  const float s = a.hi + b.hi;
+  const float v = s - a.hi;
+  float e = (a.hi - (s - v)) + (b.hi - v);
+  e += a.lo + b.lo;
+  return df_fast_two_sum(s, e);
+}
+__host__ __device__ __forceinline__ dfl operator-(dfl a) { return dfl(-a.hi, -a.lo); }
+__host__ __device__ __forceinline__ dfl operator-(dfl a, dfl b) { return a + (-b); }
+__host__ __device__ __forceinline__ dfl operator*(dfl a, dfl b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_fast_two_sum(p, e);
+}
+__host__ __device__ __forceinline__ double df_to_double(dfl a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ dfl df_from_double(double d) {
+  const float h = __double2float_rn(d);
+  return dfl(h, __double2float_rn(d - (double)h));
+}
+struct __align__(16) dcx {
+  dfl x, y;
+};
+
 template <typename T> struct CxOf;
 template <> struct CxOf<float> { typedef float2 type; };
 template <> struct CxOf<double> { typedef double2 type; };
+template <> struct CxOf<dfl> { typedef dcx type; };
+// the element type a complex array of the plan type is stored as in memory
+// (the float-float passes read and write double)
+template <typename T> struct MemOf { typedef typename CxOf<T>::type type; };
+template <> struct MemOf<dfl> { typedef double2 type; };
+// the scalar the plan's epilogue parameters are kept in
+template <typename T> struct AccOf { typedef T type; };
+template <> struct AccOf<dfl> { typedef double type; };
 
 __host__ __device__ __forceinline__ float2 cmk(float a, float b) { return make_float2(a, b); }
 __host__ __device__ __forceinline__ double2 cmk(double a, double b) { return make_double2(a, b); }
+__host__ __device__ __forceinline__ dcx cmk(dfl a, dfl b) {
+  dcx c;
+  c.x = a;
+  c.y = b;
+  return c;
+}
+
+// memory <-> computation forms of a complex value, and read-only twiddle loads
+template <typename C, typename M> __device__ __forceinline__ C cx_load(M v) { return v; }
+template <> __device__ __forceinline__ dcx cx_load<dcx, double2>(double2 v) {
+  return cmk(df_from_double(v.x), df_from_double(v.y));
+}
+__device__ __forceinline__ float2 cx_to_mem(float2 v) { return v; }
+__device__ __forceinline__ double2 cx_to_mem(double2 v) { return v; }
+__device__ __forceinline__ double2 cx_to_mem(dcx v) { return make_double2(df_to_double(v.x), df_to_double(v.y)); }
+__device__ __forceinline__ float2 ldtw(const float2 *p) { return __ldg(p); }
+__device__ __forceinline__ double2 ldtw(const double2 *p) { return __ldg(p); }
+__device__ __forceinline__ dcx ldtw(const dcx *p) {
+  const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+  return cmk(dfl(v.x, v.y), dfl(v.z, v.w));
+}
 
 template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { return cmk(a.x + b.x, a.y + b.y); }
 template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { return cmk(a.x - b.x, a.y - b.y); }

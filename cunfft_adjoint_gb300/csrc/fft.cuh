@@ -132,7 +132,7 @@ __device__ __forceinline__ void fft_stage(typename CxOf<T>::type *s, int pitch, 
       if (logNs > 0) {
         const int k = j & maskNs;
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[u][r] = cmul(v[u][r], __ldg(&tw[(r * k) << twsh]));
+        for (int r = 1; r < R; ++r) v[u][r] = cmul(v[u][r], ldtw(&tw[(r * k) << twsh]));
       }
       dftR<R>(v[u]);
     }
@@ -209,7 +209,7 @@ __device__ __forceinline__ void fstage(typename CxOf<T>::type *s, int pitch, int
       if (logNs > 0) {
         const int k = j & maskNs;
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[u][r] = cmul(v[u][r], __ldg(&tw[(r * k) << twsh]));
+        for (int r = 1; r < R; ++r) v[u][r] = cmul(v[u][r], ldtw(&tw[(r * k) << twsh]));
       }
       dftR<R>(v[u]);
     }
@@ -286,8 +286,8 @@ template <typename T> struct FftDev {
 // W_L^q for q < L from the two-level table.
 template <typename T>
 __device__ __forceinline__ typename CxOf<T>::type twiddle_L(const FftDev<T> &f, int q) {
-  if (f.logL <= 11) return __ldg(&f.twlo[q]);
-  return cmul(__ldg(&f.twhi[q >> 11]), __ldg(&f.twlo[q & 2047]));
+  if (f.logL <= 11) return ldtw(&f.twlo[q]);
+  return cmul(ldtw(&f.twhi[q >> 11]), ldtw(&f.twlo[q & 2047]));
 }
 
 // ---------------------------------------------------------------------------

@@ -25,11 +25,12 @@ template <int LOG1> __host__ __device__ constexpr int ct_pair_row(int p, int hal
 // that the epilogue's lanes, which take consecutive slots i, read rows one
 // odd pitch apart: conflict-free 8-byte shared loads.
 template <typename T, int LOG1, int LOG2, int LOGP> struct CtPairSrc {
-  const typename CxOf<T>::type *p;  // slab
+  const typename MemOf<T>::type *p;  // slab
   int p0;
   __device__ __forceinline__ typename CxOf<T>::type load(int seq, int j, int dr) const {
     // through L2: the column pass may still have been writing when this kernel started
-    return __ldcg(p + (ct_pair_row<LOG1>(p0 + (seq & ((1 << LOGP) - 1)), seq >> LOGP) << LOG2) + j + dr);
+    return cx_load<typename CxOf<T>::type>(
+        __ldcg(p + (ct_pair_row<LOG1>(p0 + (seq & ((1 << LOGP) - 1)), seq >> LOGP) << LOG2) + j + dr));
   }
 };
 
@@ -39,9 +40,11 @@ struct CtNoDst {
 
 // row-pair block `pblock` of one packed grid z; outputs Fs[0 .. nf)
 template <typename T, int LOGL>
-__device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *slab, const FftDev<T> &f,
-                                                const AccParams<T> &e, typename CxOf<T>::type *Fs, int pblock) {
+__device__ __forceinline__ void ct_rowpass_body(const typename MemOf<T>::type *slab, const FftDev<T> &f,
+                                                const AccParams<typename AccOf<T>::type> &e,
+                                                typename MemOf<T>::type *Fs, int pblock) {
   typedef typename CxOf<T>::type C;
+  typedef typename AccOf<T>::type A;
   constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
   constexpr int L2 = 1 << LOG2;
   constexpr int LOGB = ilog2c(PassCfg<T>::ELEMS) - LOG2;
@@ -57,9 +60,9 @@ __device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *sl
   pdl_trigger();
   for (int u = threadIdx.x; u < B + L2; u += THREADS) {
     const int q = u < B ? ct_pair_row<LOG1>(p0 + (u >> 1), u & 1) : (u - B) << LOG1;
-    T sn, cs;
-    sincospi_t((T)q * e.twk, &sn, &cs);
-    twr[u] = cmk(cs, sn);  // twr[B + k2] is twc[k2]
+    A sn, cs;
+    sincospi_t((A)q * e.twk, &sn, &cs);
+    twr[u] = cmk((T)cs, (T)sn);  // twr[B + k2] is twc[k2]
   }
   pdl_wait();  // the rows come from the column pass
   CtPairSrc<T, LOG1, LOG2, LOGP> src{slab, p0};
@@ -84,9 +87,9 @@ __device__ __forceinline__ void ct_rowpass_body(const typename CxOf<T>::type *sl
 // three CTAs per SM for the short rows of many small grids (bootstrap), where
 // the pass streams from HBM and more bytes in flight pay
 template <typename T, int LOGL>
-__global__ void __launch_bounds__(PassCfg<T>::THREADS, (sizeof(T) == 4 && LOGL <= 15) ? 3 : 2) k_ct_rowpass_acc(const typename CxOf<T>::type *grid,
-                                                                        FftDev<T> f, AccParams<T> e,
-                                                                        typename CxOf<T>::type *F) {
+__global__ void __launch_bounds__(PassCfg<T>::THREADS, (sizeof(T) == 4 && LOGL <= 15) ? 3 : 2) k_ct_rowpass_acc(const typename MemOf<T>::type *grid,
+                                                                        FftDev<T> f, AccParams<typename AccOf<T>::type> e,
+                                                                        typename MemOf<T>::type *F) {
   ct_rowpass_body<T, LOGL>(grid + ((int64_t)blockIdx.y << LOGL), f, e, F + (int64_t)blockIdx.y * e.nf, blockIdx.x);
 }
 

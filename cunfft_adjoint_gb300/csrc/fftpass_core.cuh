@@ -77,15 +77,15 @@ __device__ __forceinline__ void ct_stage(typename CxOf<T>::type *s, const typena
       const int step = (j & ((1 << LOGNS) - 1)) << TWSH;
       if (sizeof(T) == 8) {
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[u][r] = cmul(v[u][r], __ldg(tw + r * step));
+        for (int r = 1; r < R; ++r) v[u][r] = cmul(v[u][r], ldtw(tw + r * step));
       } else {
       C wa[4];
 #pragma unroll
-      for (int a = 1; a < (R < 4 ? R : 4); ++a) wa[a] = __ldg(tw + a * step);
+      for (int a = 1; a < (R < 4 ? R : 4); ++a) wa[a] = ldtw(tw + a * step);
 #pragma unroll
       for (int b = 0; b < R; b += 4) {
         C wb = cmk((T)1, (T)0);
-        if (b > 0) wb = __ldg(tw + b * step);
+        if (b > 0) wb = ldtw(tw + b * step);
 #pragma unroll
         for (int a = 0; a < 4 && a < R; ++a) {
           const int r = a + b;
@@ -148,15 +148,15 @@ __device__ __forceinline__ void ct_fft(typename CxOf<T>::type *s, const typename
 // (row-major L1 x L2), times W_L^{c k1}, stored in place.
 // ---------------------------------------------------------------------------
 template <typename T, int LOG1, int LOG2> struct CtColSrc {
-  const typename CxOf<T>::type *p;  // slab + c0
+  const typename MemOf<T>::type *p;  // slab + c0
   __device__ __forceinline__ typename CxOf<T>::type load(int seq, int j, int dr) const {
     // through L2: the gridding may still have been writing when this kernel started
-    return __ldcg(p + ((j + dr) << LOG2) + seq);
+    return cx_load<typename CxOf<T>::type>(__ldcg(p + ((j + dr) << LOG2) + seq));
   }
 };
 
 template <typename T, int LOG1, int LOG2, int LOGB> struct CtColDst {
-  typename CxOf<T>::type *p;              // slab + c0
+  typename MemOf<T>::type *p;             // slab + c0
   const typename CxOf<T>::type *steps;    // shared: steps[seq * 17 + r] = W_L^{c (r << LOGNS_last)}
   FftDev<T> f;
   int c0;
@@ -168,7 +168,7 @@ template <typename T, int LOG1, int LOG2, int LOGB> struct CtColDst {
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const C w = r == 0 ? w0 : cmul(w0, steps[seq * 17 + r]);
-      p[((idxD + (r << LOGNS)) << LOG2) + seq] = cmul(v[r], w);
+      p[((idxD + (r << LOGNS)) << LOG2) + seq] = cx_to_mem(cmul(v[r], w));
     }
   }
 };
@@ -182,7 +182,7 @@ template <int LOGN> __host__ __device__ constexpr int last_logns() {
 // `in` to `out` (in == out allowed: every read precedes the first barrier,
 // every write follows it)
 template <typename T, int LOGL>
-__device__ __forceinline__ void ct_colpass_body(const typename CxOf<T>::type *in, typename CxOf<T>::type *out,
+__device__ __forceinline__ void ct_colpass_body(const typename MemOf<T>::type *in, typename MemOf<T>::type *out,
                                                 const FftDev<T> &f, int cblock) {
   typedef typename CxOf<T>::type C;
   constexpr int LOG1 = (LOGL + 1) / 2, LOG2 = LOGL / 2;
@@ -207,9 +207,9 @@ __device__ __forceinline__ void ct_colpass_body(const typename CxOf<T>::type *in
 }
 
 template <typename T, int LOGL>
-__global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_colpass(typename CxOf<T>::type *grid, FftDev<T> f,
+__global__ void __launch_bounds__(PassCfg<T>::THREADS) k_ct_colpass(typename MemOf<T>::type *grid, FftDev<T> f,
                                                                     int64_t slab_stride) {
-  typename CxOf<T>::type *z = grid + blockIdx.y * slab_stride;
+  typename MemOf<T>::type *z = grid + blockIdx.y * slab_stride;
   ct_colpass_body<T, LOGL>(z, z, f, blockIdx.x);
 }
 

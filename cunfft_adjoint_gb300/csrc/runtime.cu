@@ -94,6 +94,15 @@ struct TwEntry {
 std::mutex g_tw_mu;
 std::map<std::tuple<int, int, int>, TwEntry> *g_tw = new std::map<std::tuple<int, int, int>, TwEntry>();
 
+// float-float table entries: the double value as its nearest float and the
+// remainder, laid out as the device's float-float complex (re.hi, re.lo,
+// im.hi, im.lo)
+struct DfPair {
+  float hi, lo;
+  DfPair() = default;
+  explicit DfPair(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+};
+
 template <typename T>
 int upload_table(int64_t count, int64_t step_num, int64_t denom, const void **out) {
   // entries exp(+2 pi i * q * step_num / denom), q < count, in double then rounded
@@ -102,8 +111,8 @@ int upload_table(int64_t count, int64_t step_num, int64_t denom, const void **ou
     // exact reduction of the angle numerator before the trigonometric call
     int64_t num = (q * step_num) % denom;
     double a = 2.0 * M_PI * (double)num / (double)denom;
-    h[2 * q] = (T)cos(a);
-    h[2 * q + 1] = (T)sin(a);
+    h[2 * q] = T(cos(a));
+    h[2 * q + 1] = T(sin(a));
   }
   void *d = nullptr;
   size_t bytes = sizeof(T) * h.size();
@@ -115,6 +124,34 @@ int upload_table(int64_t count, int64_t step_num, int64_t denom, const void **ou
   return CUNA2_SUCCESS;
 }
 }  // namespace
+
+int fft_geometry_df(int logL, FftGeom *g) {
+  if (logL < 2 || logL > kMaxLogL) return fail(CUNA2_ERROR_UNSUPPORTED, "FFT length 2^%d unsupported", logL);
+  int dev = 0;
+  CUNA_CK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_tw_mu);
+  auto key = std::make_tuple(dev, 4, logL);
+  auto it = g_tw->find(key);
+  if (it != g_tw->end()) {
+    *g = it->second.g;
+    return CUNA2_SUCCESS;
+  }
+  FftGeom G{};
+  G.logL = logL;
+  G.single = false;
+  G.logL1 = (logL + 1) / 2;
+  G.logL2 = logL / 2;
+  const int64_t L = int64_t(1) << logL, L1 = int64_t(1) << G.logL1, L2 = int64_t(1) << G.logL2;
+  const int64_t nlo = L < 2048 ? L : 2048, nhi = L / nlo;
+  int st;
+  if ((st = upload_table<DfPair>(L1, 1, L1, &G.tw1))) return st;
+  if ((st = upload_table<DfPair>(L2, 1, L2, &G.tw2))) return st;
+  if ((st = upload_table<DfPair>(nlo, 1, L, &G.twlo))) return st;
+  if ((st = upload_table<DfPair>(nhi, nlo, L, &G.twhi))) return st;
+  (*g_tw)[key] = TwEntry{G};
+  *g = G;
+  return CUNA2_SUCCESS;
+}
 
 int fft_geometry(bool is_double, int logL, FftGeom *g, bool split) {
   if (logL < 0 || logL > kMaxLogL) return fail(CUNA2_ERROR_UNSUPPORTED, "FFT length 2^%d unsupported", logL);
@@ -240,6 +277,14 @@ bool pdl_enabled() {
 bool masked_gather_forced() {
   static const bool on = [] {
     const char *v = getenv("CUNA2_GATHER_MASKS");
+    return v && v[0] == '1';
+  }();
+  return on;
+}
+
+bool fp64_passes_forced() {
+  static const bool on = [] {
+    const char *v = getenv("CUNA2_F64_PASSES");
     return v && v[0] == '1';
   }();
   return on;

@@ -57,6 +57,9 @@ constexpr int kMaxLogL = 26;
 // split: force the four-step L1 x L2 factorisation even where one CTA could
 // hold the whole transform (multi-CTA passes for a single small transform)
 int fft_geometry(bool is_double, int logL, FftGeom *g, bool split = false);
+// The four-step geometry of a float-float transform of length 2^logL: the
+// same tables as the double one, each entry a float-float complex.
+int fft_geometry_df(int logL, FftGeom *g);
 
 // One-time per-device setup (kernel attributes): setup_done(key) tells whether
 // `key` has been marked on the current device, mark_setup_done(key) marks it.
@@ -78,6 +81,9 @@ bool tma_enabled();
 // CUNA2_GATHER_MASKS=1: float plans keep the tap masks in the gather even
 // where the Gaussian's tail allows the unmasked form (for comparisons)
 bool masked_gather_forced();
+// CUNA2_F64_PASSES=1: double plans run their four-step passes in FP64
+// arithmetic instead of float-float (for comparisons)
+bool fp64_passes_forced();
 // Tiled 3D tensor map (CUtensorMap, 128 bytes at `map`) over float32 data at
 // `base`: dims {d0, d1, d2} (d0 innermost), byte strides {s1, s2} of
 // dimensions 1 and 2, box {b0, b1, 1}.  Returns false when the CUDA driver entry

@@ -397,6 +397,20 @@ def _spectra_under(tmp_path, tag, env, which):
     return np.load(tmp_path / (tag + ".npz"))
 
 
+def test_float_float_passes_match_fp64(tmp_path):
+    """Double plans run their four-step passes in float-float arithmetic
+    (default) or in FP64 (CUNA2_F64_PASSES=1): the same fixed-point grids give
+    spectra within 1e-13 relative L2 of each other at packed lengths 2^12 ..
+    2^22; float plans are untouched (bit-identical)."""
+    a = _spectra_under(tmp_path, "df", {"CUNA2_F64_PASSES": "0"}, "all")
+    b = _spectra_under(tmp_path, "fp64", {"CUNA2_F64_PASSES": "1"}, "all")
+    for key in a.files:
+        if "float32" in key:
+            assert np.array_equal(a[key], b[key]), key
+        else:
+            assert rel_l2(a[key], b[key]) < 1e-13, key
+
+
 def test_tma_column_pass_matches_plain(tmp_path):
     """The opt-in TMA column pass (CUNA2_TMA=1) stages its columns through
     tensor-map boxes (float packed lengths 2^13 .. 2^24 here); with
