@@ -786,12 +786,37 @@ __device__ __forceinline__ void fixed_load4(const long long *acc, int i, double 
   d = (double)v.y * inv;
 }
 
-// all 2m taps of the staged records srec[0, cnt) into the tile acc, scaled by sc
+// Tap arithmetic of the fixed-point form: float plans in float; double plans
+// in float-float on the FP32 pipe (about 48 bits, below the 2^-50 quantum's
+// reach only where a tap is far below its tile's bound), the per-record
+// factors E, Q, 1/Q and the 2m coefficients formed in double first.
+template <typename T> struct TapOf { typedef T type; };
+template <> struct TapOf<double> { typedef dfl type; };
+__device__ __forceinline__ float tap_from(float v) { return v; }
+__device__ __forceinline__ dfl tap_from(double v) { return df_from_double(v); }
+__device__ __forceinline__ int tap_fix(float w) { return FixAcc<float>::to_fix(w); }
+// round(hi + lo) for |hi + lo| <= 2^50, from the bit fields of hi: at or
+// above 2^23 hi is an integer (its 24-bit significand shifted left) and lo,
+// below half its ulp, rounds on its own; below 2^23 the float sum rounds.
+__device__ __forceinline__ long long tap_fix(dfl w) {
+  if (fabsf(w.hi) >= 8388608.0f) {
+    const int b = __float_as_int(w.hi);
+    const int sh = ((b >> 23) & 0xff) - 150;
+    const long long mag = (long long)((b & 0x7fffff) | 0x800000) << sh;
+    return (b < 0 ? -mag : mag) + (long long)__float2int_rn(w.lo);
+  }
+  return (long long)__float2int_rn(w.hi + w.lo);
+}
+
+// all 2m taps of the staged records srec[0, cnt) into the tile acc, scaled by
+// sc; cd holds the coefficients exp2(-k1 d^2) in the tap arithmetic's type
 template <typename T>
 __device__ __forceinline__ void fixed_taps(const SRec<T> *srec, int cnt, T sc, const AccParams<T> &e,
                                            const T *cd, typename FixAcc<T>::type *acc, int TL, int gmask) {
   typedef FixAcc<T> FA;
   typedef typename FA::type A;
+  typedef typename TapOf<T>::type W;
+  const W *cw = reinterpret_cast<const W *>(cd);
   const int m = e.m;
 #pragma unroll 1
   for (int i = threadIdx.x; i < cnt; i += kGridThreads) {
@@ -803,33 +828,34 @@ __device__ __forceinline__ void fixed_taps(const SRec<T> *srec, int cnt, T sc, c
     T Qi;
     if constexpr (sizeof(T) == 8) Qi = __drcp_rn(Q);
     else Qi = exp2_g(-e.k2 * q.f);
+    const W Ew = tap_from(E), Qw = tap_from(Q), Qiw = tap_from(Qi);
     const int p0 = q.lc;
     if (p0 - m + 1 >= 0 && p0 + m < TL) {  // every tap inside the tile
       A *a = acc + p0;
-      T u = E;
+      W u = Ew;
 #pragma unroll 4
       for (int d = 0; d <= m; ++d) {  // taps right of the cell, Q^d
-        FA::add(a + d, FA::to_fix(u * cd[d + m - 1]));
-        u *= Q;
+        FA::add(a + d, tap_fix(u * cw[d + m - 1]));
+        u = u * Qw;
       }
-      u = E * Qi;
+      u = Ew * Qiw;
 #pragma unroll 4
       for (int d = -1; d > -m; --d) {  // taps left of the cell
-        FA::add(a + d, FA::to_fix(u * cd[d + m - 1]));
-        u *= Qi;
+        FA::add(a + d, tap_fix(u * cw[d + m - 1]));
+        u = u * Qiw;
       }
     } else {  // near the tile edge: wrap, keep the taps inside the tile
-      T u = E;
+      W u = Ew;
       for (int d = 0; d <= m; ++d) {
         const int lc = (p0 + d) & gmask;
-        if (lc < TL) FA::add(&acc[lc], FA::to_fix(u * cd[d + m - 1]));
-        u *= Q;
+        if (lc < TL) FA::add(&acc[lc], tap_fix(u * cw[d + m - 1]));
+        u = u * Qw;
       }
-      u = E * Qi;
+      u = Ew * Qiw;
       for (int d = -1; d > -m; --d) {
         const int lc = (p0 + d) & gmask;
-        if (lc < TL) FA::add(&acc[lc], FA::to_fix(u * cd[d + m - 1]));
-        u *= Qi;
+        if (lc < TL) FA::add(&acc[lc], tap_fix(u * cw[d + m - 1]));
+        u = u * Qiw;
       }
     }
   }
@@ -878,7 +904,7 @@ __device__ __forceinline__ void grid_tile_fixed(const Src &recs, int r0, int r1,
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int d = threadIdx.x; d < 2 * m; d += kGridThreads) {
     const T dd = (T)(d - m + 1);
-    cd[d] = exp2_g(-e.k1 * dd * dd);
+    reinterpret_cast<typename TapOf<T>::type *>(cd)[d] = tap_from(exp2_g(-e.k1 * dd * dd));
   }
   // bucket histogram of the tile's records (slab independent); a record of
   // this tile lies in [base - m, base + TL + m) modulo ng
