@@ -818,17 +818,27 @@ __device__ __forceinline__ void fixed_taps(const SRec<T> *srec, int cnt, T sc, c
   typedef typename TapOf<T>::type W;
   const W *cw = reinterpret_cast<const W *>(cd);
   const int m = e.m;
+  W k1w, k2w;  // the exponent constants in the tap arithmetic
+  if constexpr (sizeof(T) == 8) {
+    k1w = df_from_double(e.k1);
+    k2w = df_from_double(e.k2);
+  }
 #pragma unroll 1
   for (int i = threadIdx.x; i < cnt; i += kGridThreads) {
     const SRec<T> q = srec[i];
-    const T E = q.y * sc * exp2_g(-e.k1 * q.f * q.f);
-    const T Q = exp2_g(e.k2 * q.f);
-    // double: 1/Q by the FP64 reciprocal, a few FP64 operations instead of a
-    // third exp2; float keeps the hardware exp2
-    T Qi;
-    if constexpr (sizeof(T) == 8) Qi = __drcp_rn(Q);
-    else Qi = exp2_g(-e.k2 * q.f);
-    const W Ew = tap_from(E), Qw = tap_from(Q), Qiw = tap_from(Qi);
+    W Ew, Qw, Qiw;
+    if constexpr (sizeof(T) == 8) {
+      // E = y sc 2^(-k1 f^2), Q = 2^(k2 f), 1/Q in float-float: only the two
+      // conversions from double use the FP64 pipe
+      const dfl fw = df_from_double(q.f);
+      Ew = df_from_double(q.y * sc) * df_exp2(-(k1w * fw * fw));
+      Qw = df_exp2(k2w * fw);
+      Qiw = df_rcp(Qw);
+    } else {
+      Ew = q.y * sc * exp2_g(-e.k1 * q.f * q.f);
+      Qw = exp2_g(e.k2 * q.f);
+      Qiw = exp2_g(-e.k2 * q.f);
+    }
     const int p0 = q.lc;
     if (p0 - m + 1 >= 0 && p0 + m < TL) {  // every tap inside the tile
       A *a = acc + p0;

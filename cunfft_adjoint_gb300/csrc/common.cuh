@@ -44,6 +44,37 @@ __device__ __forceinline__ dfl df_from_double(double d) {
   const float h = __double2float_rn(d);
   return dfl(h, __double2float_rn(d - (double)h));
 }
+// 2^x for |x| < 100 in float-float: x = n + r with n = rint(x), |r| <= 1/2,
+// 2^r = exp(r ln 2) by its Taylor series to degree 13 (the first omitted
+// term is below 2e-16 for |r ln 2| <= 0.347) in Horner form, then the exact
+// scaling by 2^n.
+__device__ __forceinline__ dfl df_exp2(dfl x) {
+  const float n = rintf(x.hi);
+  const dfl r = x - dfl(n, 0.f);
+  const dfl z = r * dfl(0.69314718055994530942);
+  dfl p = dfl(1.0 / 6227020800.0);  // 1/13!
+  p = p * z + dfl(1.0 / 479001600.0);
+  p = p * z + dfl(1.0 / 39916800.0);
+  p = p * z + dfl(1.0 / 3628800.0);
+  p = p * z + dfl(1.0 / 362880.0);
+  p = p * z + dfl(1.0 / 40320.0);
+  p = p * z + dfl(1.0 / 5040.0);
+  p = p * z + dfl(1.0 / 720.0);
+  p = p * z + dfl(1.0 / 120.0);
+  p = p * z + dfl(1.0 / 24.0);
+  p = p * z + dfl(1.0 / 6.0);
+  p = p * z + dfl(0.5);
+  p = p * z + dfl(1.0);
+  p = p * z + dfl(1.0);
+  const float s = ldexpf(1.0f, (int)n);
+  return dfl(p.hi * s, p.lo * s);
+}
+// 1/a: the float reciprocal of a.hi refined by one Newton step in float-float
+__device__ __forceinline__ dfl df_rcp(dfl a) {
+  const dfl r0(__frcp_rn(a.hi), 0.f);
+  const dfl e = dfl(1.0f, 0.f) - a * r0;
+  return r0 + r0 * e;
+}
 struct __align__(16) dcx {
   dfl x, y;
 };
