@@ -40,9 +40,24 @@ __host__ __device__ __forceinline__ dfl operator*(dfl a, dfl b) {
   return df_fast_two_sum(p, e);
 }
 __host__ __device__ __forceinline__ double df_to_double(dfl a) { return (double)a.hi + (double)a.lo; }
+// double -> float-float from the bit fields, integer and FP32 operations only:
+// hi keeps the top 24 significant bits (truncated, same sign and exponent),
+// lo the remaining 29-bit integer times 2^(e - 52), rounded to a float; hi +
+// lo is d to 2^-47 relative.  Zero, values outside the float range and
+// non-finite values take the FP64 conversions.
 __device__ __forceinline__ dfl df_from_double(double d) {
-  const float h = __double2float_rn(d);
-  return dfl(h, __double2float_rn(d - (double)h));
+  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  const int ex = (int)((u >> 52) & 0x7ff);
+  const int fe = ex - 1023 + 127;
+  if (fe <= 0 || fe >= 255) {
+    const float h = __double2float_rn(d);
+    return dfl(h, __double2float_rn(d - (double)h));
+  }
+  const unsigned sign = (unsigned)(u >> 63) << 31;
+  const unsigned long long mant = u & 0xFFFFFFFFFFFFFull;
+  const float hi = __int_as_float((int)(sign | ((unsigned)fe << 23) | (unsigned)(mant >> 29)));
+  const float lo = ldexpf(__int2float_rn((int)(mant & 0x1FFFFFFFull)), ex - 1075);
+  return dfl(hi, sign ? -lo : lo);
 }
 // 2^x for |x| < 100 in float-float: x = n + r with n = rint(x), |r| <= 1/2,
 // 2^r = exp(r ln 2) by its Taylor series to degree 13 (the first omitted
