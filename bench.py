@@ -625,6 +625,38 @@ def reference_arm(args, wl):
     print(json.dumps(line), flush=True)
 
 
+def f64_leg(dev, args, wl, ts, ys, td, stream):
+    """The same workload through a float64 plan (graph replay, one stream)."""
+    import torch
+    from cunfft_adjoint_gb300 import _lib
+    from cunfft_adjoint_gb300.nfft import AdjointNFFT
+    L = _lib.core()
+    nf, R, m, T = wl["nf"], wl["R"], wl["m"], wl["T"]
+    plan64 = AdjointNFFT(nf, R, m, torch.float64, device=dev)
+    yd64 = [torch.as_tensor(y, dtype=torch.float64, device=dev) for y in ys[:4]]
+    if not args.no_autotune:
+        plan64.autotune(td[0], yd64[0], 0.0, T, reps=2)
+    if not args.no_graph:
+        _lib.check(L.cuna2_plan_set_graph(plan64._h, 1))
+    n64 = len(yd64)
+    F64 = torch.empty(nf, dtype=torch.complex128, device=dev)
+    with torch.cuda.stream(stream):
+        for s in range(8):
+            plan64.adjoint(td[s % n64], yd64[s % n64], 0.0, T, out=F64)
+    torch.cuda.synchronize()
+    k64 = max(10, min(200, args.steps // 10))
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        a0.record(stream)
+        for s in range(k64):
+            plan64.adjoint(td[s % n64], yd64[s % n64], 0.0, T, out=F64)
+        a1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = a0.elapsed_time(a1) / k64
+    err64 = ndft_check(ts[0], ys[0], plan64.adjoint(td[0], yd64[0], 0.0, T).cpu().numpy(), nf, T)
+    return {"value": 1000.0 / ms64, "unit": UNIT, "ms_per_step": ms64, "rel_err_vs_fp64_ndft": err64, "steps": k64}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -637,7 +669,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--streams", type=int, default=3, help="concurrent streams, one plan each")
     ap.add_argument("--no-side-legs", action="store_true", help="skip the float64 and batched legs")
-    ap.add_argument("--only", choices=["bootstrap", "uneven", "autograd"],
+    ap.add_argument("--only", choices=["bootstrap", "uneven", "autograd", "f64"],
                     help="run one batched leg alone (no plain leg) and print its result")
     ap.add_argument("--nsets", type=int, default=NSETS, help="rotating input sets (default 16: 192 MB > L2)")
     ap.add_argument("--batch-schedule", default=None, metavar="LOG_TILE,FORM",
@@ -651,6 +683,13 @@ def main():
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         return reference_arm(args, wl)
+    if args.only == "f64":
+        import torch
+        dev = torch.device("cuda", 0)
+        ts, ys = make_inputs(wl, 0, 4)
+        td = [torch.as_tensor(t, device=dev) for t in ts]
+        print(json.dumps(f64_leg(dev, args, wl, ts, ys, td, torch.cuda.Stream(dev))), flush=True)
+        return
     if args.only:
         import torch
         dev = torch.device("cuda", 0)
@@ -882,30 +921,7 @@ def main():
     blocking_ms = (time.perf_counter() - b0) * 1000.0 / nb
 
     # float64 side by side (same workload, double plan)
-    f64 = None
-    if rank == 0 and not args.no_side_legs:
-        plan64 = AdjointNFFT(nf, R, m, torch.float64, device=dev)
-        yd64 = [torch.as_tensor(y, dtype=torch.float64, device=dev) for y in ys[:4]]
-        if not args.no_autotune:
-            plan64.autotune(td[0], yd64[0], 0.0, T, reps=2)
-        if not args.no_graph:
-            _lib.check(L.cuna2_plan_set_graph(plan64._h, 1))
-        n64 = len(yd64)
-        F64 = torch.empty(nf, dtype=torch.complex128, device=dev)
-        for s in range(8):
-            plan64.adjoint(td[s % n64], yd64[s % n64], 0.0, T, out=F64)
-        torch.cuda.synchronize()
-        k64 = max(10, min(200, args.steps // 10))
-        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a0.record(stream)
-        for s in range(k64):
-            plan64.adjoint(td[s % n64], yd64[s % n64], 0.0, T, out=F64)
-        a1.record(stream)
-        torch.cuda.synchronize()
-        ms64 = a0.elapsed_time(a1) / k64
-        err64 = ndft_check(ts[0], ys[0], plan64.adjoint(td[0], yd64[0], 0.0, T).cpu().numpy(), nf, T)
-        f64 = {"value": 1000.0 / ms64, "unit": UNIT, "ms_per_step": ms64, "rel_err_vs_fp64_ndft": err64,
-               "steps": k64}
+    f64 = f64_leg(dev, args, wl, ts, ys, td, stream) if rank == 0 and not args.no_side_legs else None
 
     r1 = reference_cuda_leg(dev, args.steps, wl) if rank == 0 and not args.no_side_legs else None
 
