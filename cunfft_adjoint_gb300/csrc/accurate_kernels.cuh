@@ -110,10 +110,20 @@ __device__ __forceinline__ void acc_output_tw(const AccParams<typename AccOf<T>:
   const C Ap = cadd(Zk, Zmc);
   const C Bv = cmuli(csub(Zmc, Zk));
   const C G2 = cadd(Ap, cmul(tw, Bv));
-  const A kf = (A)(int)k;
-  A sc = e.c0 * exp2_t(e.c1 * (A)1.4426950408889634 * kf * kf);
-  if (k & 1) sc = -sc;
-  const M Fk = cscale(cx_to_mem(G2), sc);
+  M Fk;
+  if constexpr (std::is_same<T, dfl>::value) {
+    // the deconvolution factor in float-float too: only the final value is
+    // rejoined in double
+    const dfl kf((float)(int)k, 0.f);  // k <= nf / 2 <= 2^24: exact
+    dfl sc = df_from_double(e.c0) * df_exp2(df_from_double(e.c1 * 1.4426950408889634) * kf * kf);
+    if (k & 1) sc = -sc;
+    Fk = cx_to_mem(cmk(G2.x * sc, G2.y * sc));
+  } else {
+    const A kf = (A)(int)k;
+    A sc = e.c0 * exp2_t(e.c1 * (A)1.4426950408889634 * kf * kf);
+    if (k & 1) sc = -sc;
+    Fk = cscale(cx_to_mem(G2), sc);
+  }
   if (k < e.K) F[e.K + k] = Fk;
   if (k >= 1) F[e.K - k] = cconj(Fk);
 }
