@@ -246,6 +246,18 @@ template <> struct FixAcc<float> {
   __device__ static int to_fix(float w) { return __float2int_rn(w); }
   __device__ static void add(int *a, int v) { atomicAdd(a, v); }
 };
+// The drop-in's tile sums (reference arithmetic) keep the widest double
+// range, 2^62 with a conversion per value: their target is the reference's
+// own FP64 result (6e-16 relative on GB300), not a kernel error.
+template <typename T> struct FixAccWide : FixAcc<T> {};
+template <> struct FixAccWide<double> {
+  typedef long long type;
+  static constexpr double range = 4611686018427387904.0;  // 2^62
+  __device__ static long long to_fix(double w) { return __double2ll_rn(w); }
+  __device__ static void add(long long *a, long long v) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(a), (unsigned long long)v);
+  }
+};
 template <> struct FixAcc<double> {
   typedef long long type;
   static constexpr double range = 1125899906842624.0;  // 2^50

@@ -169,7 +169,7 @@ __device__ __forceinline__ double rec_val(const RecD &r) { return r.v; }
 // once.  The tile's scale comes from a bound on every cell's sum: |val| <=
 // Ymax over the tile's records, a weight is at most 1 / sqrt(pi b), and at
 // most 2 hmax records reach one cell (hmax: the most records in a bucket of
-// >= 2 rf cells).  The quantum is 2^-30 (float) / 2^-50 (double) of that
+// >= 2 rf cells).  The quantum is 2^-30 (float) / 2^-62 (double) of that
 // bound, and the sums no longer depend on the order of the atomics.
 // ---------------------------------------------------------------------------
 template <typename T, bool BOOT>
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(kCompatThreads) k_grid_compat(const typename R
                                                                 const typename FpOf<T>::type *fp,
                                                                 const T *__restrict__ y, int n, unsigned seed) {
   typedef typename RecOf<T>::type Rec;
-  typedef FixAcc<T> FA;
+  typedef FixAccWide<T> FA;
   typedef typename FA::type A;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   A *acc = reinterpret_cast<A *>(smem_raw);
