@@ -7,10 +7,12 @@
 namespace cuna {
 
 // Float-float ("double-float") scalar: an unevaluated sum hi + lo of two
-// floats, |lo| <= ulp(hi) / 2, about 48 significant bits.  The float64 plan's
-// FFT passes compute in it on the FP32 pipe (GB300's FP64 rate is a small
-// fraction of its FP32 rate) and keep double in memory.  Sums by Knuth's
-// two-sum, products by an FMA-exact product (Dekker's method with fma), both
+// floats, |lo| at most about ulp(hi) (results of + and * are renormalised to
+// half an ulp; pairs split from a double by df_from_double are not), about
+// 48 significant bits.  The float64 plan's FFT passes and fixed-point taps
+// compute in it on the FP32 pipe (GB300's FP64 rate is a small fraction of
+// its FP32 rate) and keep double in memory.  Sums by Knuth's two-sum,
+// products by an FMA-exact product (Dekker's method with fma), both
 // renormalised by a fast two-sum (Dekker 1971; Hida, Li, Bailey 2001).
 struct dfl {
   float hi, lo;
