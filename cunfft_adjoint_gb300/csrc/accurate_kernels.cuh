@@ -747,7 +747,8 @@ __global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 3) k_grid_s
 // reach one cell, hmax the largest count of records in a bucket of
 // max(2m, 16) consecutive cells (a cell's 2m-cell window meets two buckets);
 // weights are <= 1.  With the sum bounded by 2^30 (float, int32 cells) or
-// 2^50 (double, int64 cells) units, the quantum is 2^-30 (2^-50) of the
+// 2^50 (double, int64 cells, as two 32-bit words where hmax <= 2048) units,
+// the quantum is 2^-30 (2^-50) of the
 // bound.  Integer sums do not depend on the order of the atomics, so the grid
 // is bit-reproducible run to run.  A non-finite value makes its tiles NaN.
 // records [c0, c0 + cnt) -> srec (values from ws when given); returns the
@@ -796,6 +797,42 @@ __device__ __forceinline__ void fixed_load4(const long long *acc, int i, double 
   d = (double)v.y * inv;
 }
 
+// Double tiles in split form: each int64 tap v enters two 32-bit integer
+// atomics instead of one 64-bit one (which measured far slower in shared
+// memory): hi[c] += floor(v / 2^20) (signed) and lo[c] += v mod 2^20
+// (unsigned), arrays of TL words each in the space of the int64 tile.  The
+// cell's sum is hi * 2^20 + lo exactly when neither array overflows: a cell
+// takes at most 2 hmax taps, so lo stays below 2 hmax 2^20 <= 2^32 for hmax
+// <= 2048, and |hi| below 2^30 + 4 hmax (each |v| <= 2^50 / (2 hmax) + 1).
+// The integer sums, hence the grid's bits, equal the int64 form's.
+constexpr int kSplitBits = 20;
+constexpr int kSplitMaxH = 2048;
+template <typename T> struct FixAdd {  // one atomic in the tile's own type
+  typename FixAcc<T>::type *acc;
+  __device__ __forceinline__ void operator()(int c, typename FixAcc<T>::type v) const {
+    FixAcc<T>::add(acc + c, v);
+  }
+};
+struct SplitAdd {
+  int *hi;
+  unsigned *lo;
+  __device__ __forceinline__ void operator()(int c, long long v) const {
+    atomicAdd(lo + c, (unsigned)v & ((1u << kSplitBits) - 1u));
+    atomicAdd(hi + c, (int)(v >> kSplitBits));
+  }
+};
+// cells [i, i + 4) of a split tile as values: 16-byte shared loads
+__device__ __forceinline__ void fixed_load4_split(const int *hi, const unsigned *lo, int i, double inv, double &a,
+                                                  double &b, double &c, double &d) {
+  const int4 h = *reinterpret_cast<const int4 *>(hi + i);
+  const uint4 l = *reinterpret_cast<const uint4 *>(lo + i);
+  constexpr long long U = 1ll << kSplitBits;
+  a = (double)((long long)h.x * U + l.x) * inv;
+  b = (double)((long long)h.y * U + l.y) * inv;
+  c = (double)((long long)h.z * U + l.z) * inv;
+  d = (double)((long long)h.w * U + l.w) * inv;
+}
+
 // Tap arithmetic of the fixed-point form: float plans in float; double plans
 // in float-float on the FP32 pipe (about 48 bits, below the 2^-50 quantum's
 // reach only where a tap is far below its tile's bound), the per-record
@@ -818,13 +855,12 @@ __device__ __forceinline__ long long tap_fix(dfl w) {
   return (long long)__float2int_rn(w.hi + w.lo);
 }
 
-// all 2m taps of the staged records srec[0, cnt) into the tile acc, scaled by
-// sc; cd holds the coefficients exp2(-k1 d^2) in the tap arithmetic's type
-template <typename T>
+// all 2m taps of the staged records srec[0, cnt) into the tile through add
+// (add(c, v): integer v into local cell c), scaled by sc; cd holds the
+// coefficients exp2(-k1 d^2) in the tap arithmetic's type
+template <typename T, class Add>
 __device__ __forceinline__ void fixed_taps(const SRec<T> *srec, int cnt, T sc, const AccParams<T> &e,
-                                           const T *cd, typename FixAcc<T>::type *acc, int TL, int gmask) {
-  typedef FixAcc<T> FA;
-  typedef typename FA::type A;
+                                           const T *cd, const Add &add, int TL, int gmask) {
   typedef typename TapOf<T>::type W;
   const W *cw = reinterpret_cast<const W *>(cd);
   const int m = e.m;
@@ -851,30 +887,29 @@ __device__ __forceinline__ void fixed_taps(const SRec<T> *srec, int cnt, T sc, c
     }
     const int p0 = q.lc;
     if (p0 - m + 1 >= 0 && p0 + m < TL) {  // every tap inside the tile
-      A *a = acc + p0;
       W u = Ew;
 #pragma unroll 4
       for (int d = 0; d <= m; ++d) {  // taps right of the cell, Q^d
-        FA::add(a + d, tap_fix(u * cw[d + m - 1]));
+        add(p0 + d, tap_fix(u * cw[d + m - 1]));
         u = u * Qw;
       }
       u = Ew * Qiw;
 #pragma unroll 4
       for (int d = -1; d > -m; --d) {  // taps left of the cell
-        FA::add(a + d, tap_fix(u * cw[d + m - 1]));
+        add(p0 + d, tap_fix(u * cw[d + m - 1]));
         u = u * Qiw;
       }
     } else {  // near the tile edge: wrap, keep the taps inside the tile
       W u = Ew;
       for (int d = 0; d <= m; ++d) {
         const int lc = (p0 + d) & gmask;
-        if (lc < TL) FA::add(&acc[lc], tap_fix(u * cw[d + m - 1]));
+        if (lc < TL) add(lc, tap_fix(u * cw[d + m - 1]));
         u = u * Qw;
       }
       u = Ew * Qiw;
       for (int d = -1; d > -m; --d) {
         const int lc = (p0 + d) & gmask;
-        if (lc < TL) FA::add(&acc[lc], tap_fix(u * cw[d + m - 1]));
+        if (lc < TL) add(lc, tap_fix(u * cw[d + m - 1]));
         u = u * Qiw;
       }
     }
@@ -897,6 +932,43 @@ __device__ __forceinline__ T fixed_scale(const float *red, int hmax) {
   T sc = B > (T)0 ? FixAcc<T>::range / B : (T)0;
   if (isinf(sc)) sc = (T)0;
   return bad ? (T)NAN : sc;
+}
+
+// the taps of srec[0, cnt) into the tile, in split form when asked (double)
+template <typename T>
+__device__ __forceinline__ void tile_taps(bool split, const SRec<T> *srec, int cnt, T sc, const AccParams<T> &e,
+                                          const T *cd, typename FixAcc<T>::type *acc, int TL, int gmask) {
+  if constexpr (sizeof(T) == 8) {
+    if (split) {
+      const SplitAdd add{reinterpret_cast<int *>(acc), reinterpret_cast<unsigned *>(acc) + TL};
+      fixed_taps<T>(srec, cnt, sc, e, cd, add, TL, gmask);
+      return;
+    }
+  }
+  fixed_taps<T>(srec, cnt, sc, e, cd, FixAdd<T>{acc}, TL, gmask);
+}
+
+// fixed-order flush of the tile: out[i] = cell i * inv (inv = 1 / scale)
+template <typename T>
+__device__ __forceinline__ void tile_flush(bool split, const typename FixAcc<T>::type *acc, int TL, T inv,
+                                           T *__restrict__ out) {
+  if constexpr (sizeof(T) == 8) {
+    if (split) {
+      const int *hi = reinterpret_cast<const int *>(acc);
+      const unsigned *lo = reinterpret_cast<const unsigned *>(acc) + TL;
+      for (int i = 4 * threadIdx.x; i < TL; i += 4 * kGridThreads) {
+        T a, b, c, d;
+        fixed_load4_split(hi, lo, i, inv, a, b, c, d);
+        store4(out + i, a, b, c, d);
+      }
+      return;
+    }
+  }
+  for (int i = 4 * threadIdx.x; i < TL; i += 4 * kGridThreads) {
+    T a, b, c, d;
+    fixed_load4(acc, i, inv, a, b, c, d);
+    store4(out + i, a, b, c, d);
+  }
 }
 
 template <typename T, class Src>
@@ -971,15 +1043,11 @@ __device__ __forceinline__ void grid_tile_fixed(const Src &recs, int r0, int r1,
 #pragma unroll
     for (int w = 0; w < kGridThreads / 32; ++w) hmax = max(hmax, redi[w]);
     const T sc = fixed_scale<T>(red, hmax);
-    if (sc > (T)0) fixed_taps<T>(srec, cnt, sc, e, cd, acc, TL, gmask);
+    const bool split = sizeof(T) == 8 && hmax <= kSplitMaxH;
+    if (sc > (T)0) tile_taps<T>(split, srec, cnt, sc, e, cd, acc, TL, gmask);
     __syncthreads();
-    T *out = grid + (int64_t)sbeg * slab_stride + base;
     const T inv = sc > (T)0 ? (T)1 / sc : (sc == sc ? (T)0 : sc);
-    for (int i = 4 * threadIdx.x; i < TL; i += 4 * kGridThreads) {
-      T a, b, c, d;
-      fixed_load4(acc, i, inv, a, b, c, d);
-      store4(out + i, a, b, c, d);
-    }
+    tile_flush<T>(split, acc, TL, inv, grid + (int64_t)sbeg * slab_stride + base);
     return;
   }
   __syncthreads();
@@ -995,6 +1063,7 @@ __device__ __forceinline__ void grid_tile_fixed(const Src &recs, int r0, int r1,
   hmax = 0;
 #pragma unroll
   for (int w = 0; w < kGridThreads / 32; ++w) hmax = max(hmax, redi[w]);
+  const bool split = sizeof(T) == 8 && hmax <= kSplitMaxH;
   for (int slab = sbeg; slab < send; ++slab) {
     const T *ws = wts ? wts + (int64_t)slab * nvals : nullptr;
     float ym = 0.f;
@@ -1026,17 +1095,12 @@ __device__ __forceinline__ void grid_tile_fixed(const Src &recs, int r0, int r1,
         fixed_stage<T>(recs, c0, cnt, base, ws, srec);
         __syncthreads();
       }
-      if (sc > (T)0) fixed_taps<T>(srec, cnt, sc, e, cd, acc, TL, gmask);
+      if (sc > (T)0) tile_taps<T>(split, srec, cnt, sc, e, cd, acc, TL, gmask);
     }
     __syncthreads();
     // fixed-order flush: cell = integer / scale
-    T *out = grid + (int64_t)slab * slab_stride + base;
     const T inv = sc > (T)0 ? (T)1 / sc : (sc == sc ? (T)0 : sc);
-    for (int i = 4 * threadIdx.x; i < TL; i += 4 * kGridThreads) {
-      T a, b, c, d;
-      fixed_load4(acc, i, inv, a, b, c, d);
-      store4(out + i, a, b, c, d);
-    }
+    tile_flush<T>(split, acc, TL, inv, grid + (int64_t)slab * slab_stride + base);
   }
 }
 

@@ -256,11 +256,17 @@ def test_fixed_point_single_read_tiles(nfft, oracle_lib, dtype):
     denser tiles and weighted slabs (multi-channel) take the chunked path.
     Sparse samples with one dense burst give tiles of both kinds; channel 0
     of a multi-channel transform with values [y, 2y] runs the chunked path on
-    the same records, so it must reproduce the plain transform's bits."""
+    the same records, so it must reproduce the plain transform's bits.  In
+    double a cluster of 5000 samples inside one cell puts more than 2048
+    records in a bucket: the tiles there keep one 64-bit atomic per tap, the
+    others split each tap into two 32-bit atomics.  (In float such a
+    cluster coarsens its tile's 2^-30 quantum past the 1e-5 bar.)"""
     from cunfft_adjoint_gb300 import _lib
     rng = np.random.default_rng(41)
     nf, T = 1 << 17, 100.0
     t = np.concatenate([rng.uniform(0, T, 20_000), rng.uniform(40.0, 40.5, 6000)])
+    if dtype == torch.float64:
+        t = np.concatenate([t, rng.uniform(70.0, 70.0001, 5000)])
     y = rng.normal(0, 1, t.size)
     td = torch.as_tensor(t, device="cuda")
     yd = torch.as_tensor(y, dtype=dtype, device="cuda")
