@@ -1105,7 +1105,7 @@ __device__ __forceinline__ void grid_tile_fixed(const Src &recs, int r0, int r1,
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 2) k_grid_fixed(
+__global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 4) k_grid_fixed(
     const typename RecOf<T>::type *recs, const int *off, T *grid, AccParams<T> e, const T *wts, int64_t nvals,
     int nslab, int group, int64_t slab_stride) {
   pdl_trigger();

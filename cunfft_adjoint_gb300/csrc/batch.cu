@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(512) k_bscatter(const double *__restrict__ t, 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 2) k_bgrid(
+__global__ void __launch_bounds__(kGridThreads, sizeof(T) == 4 ? 6 : 4) k_bgrid(
     const typename RecOf<T>::type *__restrict__ recs, const int *__restrict__ off, T *__restrict__ grid,
     const BDesc<T> *__restrict__ D, const int *__restrict__ tile_series) {
   const int gt = blockIdx.x;
