@@ -61,30 +61,49 @@ __device__ __forceinline__ dfl df_from_double(double d) {
   const float lo = ldexpf(__int2float_rn((int)(mant & 0x1FFFFFFFull)), ex - 1075);
   return dfl(hi, sign ? -lo : lo);
 }
-// 2^x for |x| < 100 in float-float: x = n + r with n = rint(x), |r| <= 1/2,
-// 2^r = exp(r ln 2) by its Taylor series to degree 13 (the first omitted
-// term is below 2e-16 for |r ln 2| <= 0.347) in Horner form, then the exact
-// scaling by 2^n.
+// 2^(j/64), j = 0..63, as float-float pairs (hi, lo): the value to 1.5e-15
+// relative (2^-49), from 200-bit arithmetic
+__device__ const float2 kDfExp2Tab[64] = {
+    {0x1p+0f, 0.0f}, {0x1.02c9a4p+0f, -0x1.887fap-28f}, {0x1.059b0ep+0f, -0x1.9d4f52p-25f}, {0x1.087452p+0f, -0x1.e2990ep-26f},
+    {0x1.0b5586p+0f, 0x1.9f3122p-25f}, {0x1.0e3ec4p+0f, -0x1.a585ccp-25f}, {0x1.11301ep+0f, -0x1.fdb496p-25f}, {0x1.1429aap+0f, 0x1.d525bcp-25f},
+    {0x1.172b84p+0f, -0x1.c15742p-27f}, {0x1.1a35bep+0f, 0x1.6df96ep-25f}, {0x1.1d4874p+0f, -0x1.d2e8cap-25f}, {0x1.2063b8p+0f, 0x1.0c519ap-25f},
+    {0x1.2387a6p+0f, 0x1.ceac48p-25f}, {0x1.26b456p+0f, 0x1.789f38p-26f}, {0x1.29e9ep+0f, -0x1.5c0424p-25f}, {0x1.2d285ap+0f, 0x1.b900c2p-26f},
+    {0x1.306fep+0f, 0x1.4636e2p-25f}, {0x1.33c08cp+0f, -0x1.b37d2p-25f}, {0x1.371a74p+0f, -0x1.18aac6p-25f}, {0x1.3a7db4p+0f, -0x1.634c02p-25f},
+    {0x1.3dea64p+0f, 0x1.824684p-25f}, {0x1.4160a2p+0f, 0x1.f72e2ap-28f}, {0x1.44e086p+0f, 0x1.8624b4p-30f}, {0x1.486a2cp+0f, -0x1.47d866p-25f},
+    {0x1.4bfdaep+0f, -0x1.593abcp-25f}, {0x1.4f9b28p+0f, -0x1.2c5a6cp-25f}, {0x1.5342b6p+0f, -0x1.2c561p-25f}, {0x1.56f474p+0f, -0x1.295b04p-25f},
+    {0x1.5ab07ep+0f, -0x1.5bd5ecp-27f}, {0x1.5e76f2p+0f, -0x1.4a5bd6p-25f}, {0x1.6247ecp+0f, -0x1.f8b55p-25f}, {0x1.662388p+0f, 0x1.2a9112p-27f},
+    {0x1.6a09e6p+0f, 0x1.9fcef4p-26f}, {0x1.6dfb24p+0f, -0x1.cd72e8p-27f}, {0x1.71f75ep+0f, 0x1.1d8beep-25f}, {0x1.75feb6p+0f, -0x1.37b306p-25f},
+    {0x1.7a1148p+0f, -0x1.829fdp-25f}, {0x1.7e2f34p+0f, -0x1.261634p-25f}, {0x1.82589ap+0f, -0x1.accc7cp-26f}, {0x1.868d9ap+0f, -0x1.2edb44p-26f},
+    {0x1.8ace54p+0f, 0x1.15506ep-27f}, {0x1.8f1aeap+0f, -0x1.baa232p-26f}, {0x1.93737cp+0f, -0x1.e64744p-25f}, {0x1.97d82ap+0f, -0x1.0d8d84p-31f},
+    {0x1.9c4918p+0f, 0x1.51f848p-27f}, {0x1.a0c668p+0f, -0x1.2886a6p-26f}, {0x1.a5503cp+0f, -0x1.b83b54p-25f}, {0x1.a9e6b6p+0f, -0x1.50c048p-25f},
+    {0x1.ae89fap+0f, -0x1.a94b14p-26f}, {0x1.b33a2cp+0f, -0x1.ec3a82p-26f}, {0x1.b7f77p+0f, -0x1.a09438p-25f}, {0x1.bcc1eap+0f, -0x1.f687c6p-25f},
+    {0x1.c199bep+0f, -0x1.3d56b2p-27f}, {0x1.c67f12p+0f, 0x1.cafa2ap-25f}, {0x1.cb720ep+0f, -0x1.8837ccp-27f}, {0x1.d072d4p+0f, 0x1.40f13p-25f},
+    {0x1.d5818ep+0f, -0x1.822dbcp-27f}, {0x1.da9e6p+0f, 0x1.ed9942p-27f}, {0x1.dfc974p+0f, -0x1.908c94p-25f}, {0x1.e502eep+0f, 0x1.e2cffep-26f},
+    {0x1.ea4afap+0f, 0x1.52486cp-27f}, {0x1.efa1bep+0f, 0x1.cc2b44p-25f}, {0x1.f50766p+0f, -0x1.246ebp-26f}, {0x1.fa7c18p+0f, 0x1.9e90d8p-28f},
+};
+// 2^x for |x| < 100 in float-float, table-driven (Tang 1989): x = n + j/64
+// + r with k = 64 n + j = rint(64 x), |r| <= 1/128 (r = x - k/64 exactly
+// in its high part); 2^(j/64) = t from the table; 2^r - 1 = e^z - 1,
+// z = r ln 2, |z| < 0.0055, as z + z^2 s with s = 1/2 + z/6 + z^2/24 +
+// z^3/120 (truncation below 4e-17; the z/6 term in float-float, the rest in
+// float); 2^(j/64 + r) as t + t (2^r - 1), whose product is below 0.006 of
+// the sum; then the exact scaling by 2^n.  Relative error below 7e-15
+// (about 2^-47), checked against 120-bit arithmetic over |x| < 100.
 __device__ __forceinline__ dfl df_exp2(dfl x) {
-  const float n = rintf(x.hi);
-  const dfl r = x - dfl(n, 0.f);
+  const float kf = rintf(x.hi * 64.0f);
+  const int k = (int)kf;
+  const dfl r = x - dfl(kf * 0.015625f, 0.f);
   const dfl z = r * dfl(0.69314718055994530942);
-  dfl p = dfl(1.0 / 6227020800.0);  // 1/13!
-  p = p * z + dfl(1.0 / 479001600.0);
-  p = p * z + dfl(1.0 / 39916800.0);
-  p = p * z + dfl(1.0 / 3628800.0);
-  p = p * z + dfl(1.0 / 362880.0);
-  p = p * z + dfl(1.0 / 40320.0);
-  p = p * z + dfl(1.0 / 5040.0);
-  p = p * z + dfl(1.0 / 720.0);
-  p = p * z + dfl(1.0 / 120.0);
-  p = p * z + dfl(1.0 / 24.0);
-  p = p * z + dfl(1.0 / 6.0);
-  p = p * z + dfl(0.5);
-  p = p * z + dfl(1.0);
-  p = p * z + dfl(1.0);
-  const float s = ldexpf(1.0f, (int)n);
-  return dfl(p.hi * s, p.lo * s);
+  const dfl c6 = z * dfl(1.0 / 6.0);
+  const float u2 = (z.hi * z.hi) * fmaf(z.hi, 1.0f / 120.0f, 1.0f / 24.0f);
+  dfl s = df_fast_two_sum(0.5f, c6.hi);
+  s = df_fast_two_sum(s.hi, s.lo + (c6.lo + u2));
+  const dfl em1 = z + (z * z) * s;
+  const float2 tt = __ldg(&kDfExp2Tab[k & 63]);
+  const dfl t(tt.x, tt.y);
+  const dfl v = t + t * em1;
+  const float sc = __int_as_float((127 + (k >> 6)) << 23);  // 2^n, |n| <= 100
+  return dfl(v.hi * sc, v.lo * sc);
 }
 // 1/a: the float reciprocal of a.hi refined by one Newton step in float-float
 __device__ __forceinline__ dfl df_rcp(dfl a) {
