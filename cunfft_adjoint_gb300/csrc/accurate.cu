@@ -963,8 +963,8 @@ extern "C" int cuna2_plan_create_auto(cuna2_plan *plan, int dtype, int64_t nf, d
                                       const void *y, void *F, int64_t n, double t0, double T, cudaStream_t st,
                                       int *R_out, int *m_out) {
   clear_error();
+  if (plan) *plan = nullptr;
   if (!plan || !F || !(tol > 0) || !(tol < 1)) return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
-  *plan = nullptr;
   // the Gaussian kernel's error is about exp(-pi m sqrt(1 - 1/R)); float
   // plans cannot go below their rounding, so the target is clamped there
   const double target = std::max(tol, dtype == CUNA2_F32 ? 1e-7 : 1e-15);

@@ -701,9 +701,9 @@ extern "C" int cuna2_batch_plan_create_auto(cuna2_batch_plan *plan, int dtype, i
                                             const double *t, const void *y, void *F, cudaStream_t st, int *R_out,
                                             int *m_out) {
   clear_error();
+  if (plan) *plan = nullptr;
   if (!plan || !n || !nf || nseries < 1 || !t || !y || !F || !(tol > 0) || !(tol < 1))
     return fail(CUNA2_ERROR_INVALID_VALUE, "invalid argument");
-  *plan = nullptr;
   if (dtype != CUNA2_F32 && dtype != CUNA2_F64) return fail(CUNA2_ERROR_INVALID_VALUE, "dtype %d", dtype);
   const double target = std::max(tol, dtype == CUNA2_F32 ? 1e-7 : 1e-15);
   auto width = [&](int R) {
