@@ -333,7 +333,7 @@ def autograd_leg(dev, steps):
 
     plain_step()
     torch.cuda.synchronize()
-    kp = max(3, min(10, steps // 200))
+    kp = max(5, min(20, steps // 100))
     a0.record()
     for _ in range(kp):
         plain_step()
